@@ -1,0 +1,350 @@
+"""Benchmark of the Spiral answer path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
+
+Workload: the plain single-query answer against a 1 GiB database (n = 2,
+p = 256, nu1 = 9, nu2 = 8: 2^17 records of 8 KiB, an 8 GiB CRT-NTT image
+on the device), d = 2048, q = 268369921 * 249561089, t_exp = 8, t_gsw = 7,
+t_conv = 4.  A step answers one query.  Synthetic seeded data: uniform u8
+records, a seeded client (discrete Gaussian secret, sigma 6.4) and a query
+for a seeded random record.  The database image (8 GiB) is larger than L2,
+so every step streams it from HBM.
+
+Printed as one JSON line (rank 0):
+  value   queries/s with the query already on the device (staged), timed with
+          CUDA events over K back-to-back answers on the library's stream
+  e2e     queries/s through sp_answer with host buffers (query H2D, response
+          D2H inside the timed region), host wall clock
+  roofline  first-dimension multiply: algorithmic bytes / CUDA-event launch
+          time against the measured HBM copy bandwidth
+  cpu_baseline  the CPU oracle on this host's cores, on a bounded sample of
+          the same workload, extrapolated to queries/s
+With --gpus N > 1 (torchrun), every rank answers its own queries against its
+own replica of the database ("replicas only": the path does not shard here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "gpu-pir_gb300"))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "1GiB DB single-query answers/s (Spiral PIR, GPU)"
+UNIT = "queries/s"
+WORKLOAD = {"workload": "spiral-answer-1gib", "db_plain_bytes": 1 << 30, "db_device_bytes": 8 << 30,
+            "records": 1 << 17, "record_bytes": 8192, "n": 2, "p": 256, "nu1": 9, "nu2": 8,
+            "d": 2048, "t_exp": 8, "t_gsw": 7, "t_conv": 4, "batch": 1,
+            "l2": "database image (8 GiB) larger than L2 (129 MB); no flush needed"}
+THROTTLE = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown",
+            0x4: "sw_power_cap", 0x80: "hw_power_brake_slowdown", 0x1: "gpu_idle",
+            0x2: "applications_clocks_setting", 0x100: "display_clock_setting"}
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        cmd = ["nvidia-smi", "-i", str(self.index),
+               "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active",
+               "--format=csv,noheader,nounits", "-lms", "200"]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return self
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 4:
+                try:
+                    self.samples.append((float(parts[0]), float(parts[1]), float(parts[2]), int(parts[3], 16)))
+                except ValueError:
+                    pass
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        if not self.samples:
+            return None
+        sm = sorted(s[0] for s in self.samples)
+        reasons = set()
+        for s in self.samples:
+            for bit, name in THROTTLE.items():
+                if s[3] & bit and name not in ("gpu_idle",):
+                    reasons.add(name)
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(s[1] for s in self.samples),
+                "power_w_max": max(s[2] for s in self.samples), "samples": len(self.samples),
+                "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per multiply launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "db_mul_1gib.md")
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.strip().startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def make_workload(seed: int = 0):
+    from spiralpir import client as C
+    from spiralpir import params as P
+
+    p, sh = P.PARAMS, P.SHAPE_1GIB
+    cl = C.Client(p, seed=seed + 1)
+    keys = cl.public_keys(sh.nu1, sh.nu2)
+    recs = C.random_records(sh, p, seed=seed + 2)
+    rng = np.random.default_rng(seed + 3)
+    idx = [int(x) for x in rng.integers(0, sh.num_records, size=8)]
+    queries = [cl.query(sh, i) for i in idx]
+    return p, sh, cl, keys, recs, idx, queries
+
+
+def cpu_baseline(threads: int | None = None) -> dict:
+    """Time the CPU oracle on a bounded sample of the 1 GiB answer and
+    extrapolate to one full query: full expansion and conversion, the
+    first-dimension multiply over 8 of 256 columns (x32), the fold of
+    2^3-column instances (x255/7) and the packing."""
+    import oracle as O
+
+    rng = np.random.default_rng(9)
+
+    def residues(shape):
+        out = np.empty(tuple(shape) + (2, 2048), dtype=np.uint32)
+        out[..., 0, :] = rng.integers(0, O.Q1, size=tuple(shape) + (2048,), dtype=np.uint32)
+        out[..., 1, :] = rng.integers(0, O.Q2, size=tuple(shape) + (2048,), dtype=np.uint32)
+        return out
+
+    if threads:
+        O.set_threads(threads)
+    nth = O.num_threads()
+    n, nu1, nu2, tl, tg, tc = 2, 9, 8, 8, 7, 4
+    g = O.expansion_g(nu1, nu2, tg)
+    stop = O.expansion_stop(nu2, tg)
+    q = residues((2,))
+    left = residues((g, 2, tl))
+    right = residues((stop + 1, 2, tl))
+    t0 = time.perf_counter()
+    v = O.expand(q, left, tl, right, tl, nu1, nu2, tg)
+    t_exp = time.perf_counter() - t0
+    regev = np.ascontiguousarray(v[1:2 * nu2 * tg:2])
+    conv = residues((2, 2 * tc))
+    t0 = time.perf_counter()
+    gsw = O.regev_to_gsw(regev, conv, nu2, tg, tc)
+    neg = O.gsw_neg(gsw, tg)
+    t_conv = time.perf_counter() - t0
+    sample_cols = 3
+    db = residues((4, 1 << sample_cols, 1 << nu1))
+    sel = np.ascontiguousarray(v[0:2 << nu1:2])
+    t0 = time.perf_counter()
+    acc = O.db_mul(db, sel, 4, nu1, sample_cols)
+    raw = O.from_ntt(acc)
+    t_mul = (time.perf_counter() - t0) * (1 << (nu2 - sample_cols))
+    t0 = time.perf_counter()
+    folded = O.fold(raw, gsw[-sample_cols:], neg[-sample_cols:], sample_cols, tg)
+    t_fold = (time.perf_counter() - t0) * ((1 << nu2) - 1) / ((1 << sample_cols) - 1)
+    keys = residues((n, n + 1, tc))
+    t0 = time.perf_counter()
+    packed = O.pack(folded, keys, n, tc)
+    O.encode_response(packed, n, 8, 22)
+    t_pack = time.perf_counter() - t0
+    per_query = t_exp + t_conv + t_mul + t_fold + t_pack
+    return {"value": 1.0 / per_query, "unit": UNIT, "cores": nth, "kind": "port",
+            "seconds_per_query": per_query,
+            "stages_s": {"expand": t_exp, "convert": t_conv, "db_mul": t_mul, "fold": t_fold, "pack": t_pack},
+            "sample": "C oracle (OpenMP) on one 1 GiB-shape query: full expansion (g=10) and conversion; "
+                      "first-dimension multiply over 8 of 256 columns scaled x32; fold of 8-column "
+                      "instances scaled by 255/7 folds; packing"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    ts = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline()
+        if i >= args.warmup:
+            ts.append(r["seconds_per_query"])
+    per = sum(ts) / len(ts)
+    cb = cpu_baseline.__doc__
+    line = {"metric": METRIC, "value": 1.0 / per, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32 (exact modular)", "data": "synthetic", "config": WORKLOAD,
+            "impl": "reference",
+            "cpu_baseline": {"value": 1.0 / per, "unit": UNIT, "cores": r["cores"], "kind": "port",
+                             "sample": r["sample"]},
+            "e2e": {"value": 1.0 / per, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": " ".join(cb.split()) if cb else ""}
+    print(json.dumps(line), flush=True)
+
+
+def run_gpu(args, rank, world, local):
+    from spiralpir.lib import SpiralGPU
+
+    p, sh, cl, keys, recs, idx, queries = make_workload(seed=rank)
+    batch = args.batch
+    gpu = SpiralGPU(p, max_batch=max(batch, 1))
+    gpu.set_client_keys(1, keys)
+    t0 = time.perf_counter()
+    gpu.load_db(1, recs, sh.nu1, sh.nu2)
+    load_s = time.perf_counter() - t0
+    # correctness of the measured configuration
+    resp = gpu.answer(1, 1, queries[0])
+    ok = bool(np.array_equal(cl.decode(resp), recs[idx[0]]))
+    if not ok:
+        raise SystemExit("decoded record differs from the database record")
+    barrier = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        barrier = dist.barrier
+    # warm-up (answers through the public API, then staged runs); answering
+    # reuses the slots, so the queries are staged after it
+    for i in range(args.warmup):
+        gpu.answer(1, 1, queries[i % len(queries)])
+    for s in range(batch):
+        gpu.stage_query(s, 1, 1, queries[s % len(queries)])
+    gpu.time_staged(batch, args.warmup)
+    # device-resident timed region
+    if barrier:
+        barrier()
+    clocks = ClockSampler(local).start()
+    gpu.stats_reset()
+    ms = gpu.time_staged(batch, args.steps)
+    st = gpu.stats()
+    launches_per_answer = st["launches"] / max(1, args.steps)
+    # first-dimension multiply alone (roofline): CUDA events around its launches
+    mul_ms = gpu.time_db_mul(1, batch, max(args.steps, 5))
+    # end to end through the public API (host buffers)
+    lat = []
+    out = np.empty(gpu.response_bytes, dtype=np.uint8)
+    t_e2e = time.perf_counter()
+    for i in range(args.steps):
+        t1 = time.perf_counter()
+        gpu.answer(1, 1, queries[i % len(queries)], out=out)
+        lat.append(time.perf_counter() - t1)
+    e2e_s = time.perf_counter() - t_e2e
+    clk = clocks.stop()
+    if barrier:
+        barrier()
+    # batched answering (B queries per pipeline run), same database
+    batched = None
+    if args.batched > 1:
+        gpu2 = SpiralGPU(p, max_batch=args.batched)
+        gpu2.set_client_keys(1, keys)
+        gpu2.load_db(1, recs, sh.nu1, sh.nu2)
+        for s in range(args.batched):
+            gpu2.stage_query(s, 1, 1, queries[s % len(queries)])
+        gpu2.time_staged(args.batched, 1)
+        bms = gpu2.time_staged(args.batched, max(2, args.steps // 4))
+        rb = gpu2.fetch_response(3 % args.batched)
+        assert np.array_equal(cl.decode(rb), recs[idx[3 % args.batched % len(idx)]])
+        batched = {"B": args.batched, "queries_per_s": args.batched / (bms / 1e3),
+                   "ms_per_batch": bms, "speedup_vs_single": (args.batched / bms) / (batch / ms)}
+        gpu2.close()
+
+    value = batch * 1e3 / ms * world
+    algo_bytes = sh.num_records * p.T * 2048 * 8 + (sh.rows * 2048 * 16 + p.T * sh.cols * 4 * 2048 * 4) * batch
+    peak, peak_kind = measured_peaks()
+    achieved = algo_bytes / (mul_ms / 1e3) / 1e9
+    traffic = ncu_traffic()
+    lat_ms = sorted(x * 1e3 for x in lat)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / batch, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32 (exact modular)",
+            "data": "synthetic (seeded records, client and query)", "config": WORKLOAD,
+            "e2e": {"value": args.steps / e2e_s * world, "unit": UNIT, "h2d_bytes_per_step": 4 * 2048 * 8,
+                    "d2h_bytes_per_step": int(gpu.response_bytes),
+                    "p50_ms": lat_ms[len(lat_ms) // 2], "p99_ms": lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))]},
+            "roofline": {"bound": "hbm", "kernel": "k_db_mul", "achieved": achieved, "peak": peak,
+                         "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": algo_bytes, "launch_ms": mul_ms,
+                         "traffic": traffic},
+            "stages_ms": {k[3:]: st[k] / max(1, args.steps) for k in
+                          ("ms_expand", "ms_convert", "ms_db_mul", "ms_fold", "ms_pack", "ms_total")},
+            "gpu_launches": int(st["launches"]), "launches_per_answer": launches_per_answer,
+            "batched": batched, "clocks": clk, "db_load_s": load_s, "decoded_ok": ok}
+    if rank == 0:
+        line["cpu_baseline"] = cpu_baseline()
+    gpu.close()
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        line["ms_per_step"] = float(t.item()) / batch
+        line["value"] = batch * 1e3 / float(t.item()) * world
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
+    ap.add_argument("--batch", type=int, default=1, help="queries per step (1 = plain single-query path)")
+    ap.add_argument("--batched", type=int, default=32, help="also measure a B-query batch (0 to skip)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    run_gpu(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,561 @@
+// Query-dependent stages of the answer path: expansion, Regev->GSW
+// conversion, folding, packing, modulus switching and serialisation.
+//
+// CTA shape everywhere: 256 threads = two NTT groups of 128; group g works
+// modulo prime g.  Raw (56-bit) values are rebuilt by an inverse CRT of both
+// groups' INTT outputs exchanged through shared memory.
+#include "answer.cuh"
+
+namespace sp {
+
+namespace {
+
+constexpr int THREADS = 256;
+// shared memory: 4 twiddle tables + per group 2 transpose buffers
+constexpr int SMEM_WORDS = 4 * D + 2 * 2 * D;
+constexpr int SMEM_BYTES = SMEM_WORDS * 4;
+
+struct Ctx {
+    uint32_t *tw;    // 4 tables
+    uint32_t *buf;   // this group's two transpose buffers
+    uint32_t *bufs;  // both groups' buffers (exchange area, 4*D words)
+    Prime c;
+    int g, t, bar;
+};
+
+__device__ __forceinline__ Ctx setup(uint32_t *smem, const TwiddleSet *tws) {
+    load_twiddles(smem, tws);
+    Ctx x;
+    x.g = threadIdx.x >> 7;
+    x.t = threadIdx.x & (GROUP - 1);
+    x.c = prime_of(x.g);
+    x.tw = smem;
+    x.bufs = smem + 4 * D;
+    x.buf = x.bufs + x.g * 2 * D;
+    x.bar = 1 + x.g;
+    __syncthreads();
+    return x;
+}
+
+__device__ __forceinline__ const uint32_t *tw_fwd(const Ctx &x) { return x.tw + x.g * D; }
+__device__ __forceinline__ const uint32_t *tw_inv(const Ctx &x) { return x.tw + (2 + x.g) * D; }
+
+// Both groups hold unscaled INTT outputs (layout A, < 2p) of the same
+// polynomial mod their prime; returns the raw coefficients of this thread's
+// layout-A positions (identical in both groups).  Uses the first buffer of
+// each group as the exchange area; ends with a CTA barrier so the buffers
+// are free again.
+__device__ __forceinline__ void exchange_icrt(const Ctx &x, const uint32_t (&v)[VPT], uint64_t (&raw)[VPT]) {
+    uint32_t *mine = x.bufs + x.g * 2 * D;
+#pragma unroll
+    for (int j = 0; j < VPT; j++) mine[x.t + GROUP * j] = v[j];
+    __syncthreads();
+    const uint32_t *a0 = x.bufs, *a1 = x.bufs + 2 * D;
+#pragma unroll
+    for (int j = 0; j < VPT; j++) {
+        const int e = x.t + GROUP * j;
+        raw[j] = icrt(a0[e], a1[e]);
+    }
+    __syncthreads();
+}
+
+// acc (layout C, < 2p) += ntt (< 4p) * key (Montgomery, canonical)
+__device__ __forceinline__ void mac16(uint32_t (&acc)[VPT], const uint32_t (&v)[VPT], const uint32_t *key,
+                                      const Prime &c) {
+    uint32_t w[VPT];
+    ld16(w, key);
+#pragma unroll
+    for (int j = 0; j < VPT; j++) acc[j] = reduce2(acc[j] + mont_mul(v[j], w[j], c.p, c.pinv), 2 * c.p);
+}
+
+__device__ __forceinline__ void digits(uint32_t (&d)[VPT], const uint64_t (&raw)[VPT], int shift, uint64_t mask) {
+#pragma unroll
+    for (int j = 0; j < VPT; j++) d[j] = (uint32_t)((raw[j] >> shift) & mask);
+}
+
+__device__ __forceinline__ uint32_t to_mont(uint32_t x, const Prime &c) {  // canonical -> canonical Montgomery
+    uint32_t y = mont_mul(x, c.r2, c.p, c.pinv);
+    return min(y, y - c.p);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------ conversions
+__global__ void k_narrow(const uint64_t *__restrict__ in, uint32_t *__restrict__ out, uint64_t total, int to_m) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const Prime c = prime_of((int)((i / D) & 1));
+        uint32_t x = (uint32_t)(in[i] % c.p);
+        out[i] = to_m ? to_mont(x, c) : x;
+    }
+}
+
+__global__ void k_widen(const uint32_t *__restrict__ in, uint64_t *__restrict__ out, uint64_t total, int from_m) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const Prime c = prime_of((int)((i / D) & 1));
+        uint32_t x = in[i];
+        if (from_m) {
+            x = mont_mul(x, 1u, c.p, c.pinv);
+            x = min(x, x - c.p);
+        }
+        out[i] = x;
+    }
+}
+
+cudaError_t launch_narrow(const uint64_t *in, uint32_t *out, uint64_t planes, bool to_mont, cudaStream_t st) {
+    const uint64_t total = planes * D;
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > 8192) blocks = 8192;
+    if (blocks < 1) blocks = 1;
+    k_narrow<<<blocks, 256, 0, st>>>(in, out, total, to_mont ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_widen(const uint32_t *in, uint64_t *out, uint64_t planes, bool from_mont, cudaStream_t st) {
+    const uint64_t total = planes * D;
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > 8192) blocks = 8192;
+    if (blocks < 1) blocks = 1;
+    k_widen<<<blocks, 256, 0, st>>>(in, out, total, from_mont ? 1 : 0);
+    return cudaGetLastError();
+}
+
+// -------------------------------------------------------------- expansion
+// Round r for output index i = blockIdx.x of query blockIdx.y
+// (gpu-pir/expansion.cuh:87-166 semantics): the input is v[i] for i < 2^r
+// and x^(-2^r) * v[i - 2^r] above; the output is
+//   v + [0; tau(v).row1] + W_r * NTT(G^-1(raw(tau(v).row0)))
+// with tau = x -> x^(D/2^r + 1) applied as a slot permutation in NTT form.
+__global__ void __launch_bounds__(THREADS) k_expand_round(const QDesc *__restrict__ qd, int r, StageParams sp,
+                                                         const TwiddleSet *__restrict__ tws,
+                                                         const uint32_t *__restrict__ neg1) {
+    const QDesc &Q = qd[blockIdx.y];
+    const int i = blockIdx.x;
+    if (!Q.active || r >= Q.g || i >= (2 << r)) return;
+    const int max_bits = sp.t_gsw * Q.nu2;
+    if (Q.stop > 0 && r > Q.stop && (i & 1)) return;
+    if (Q.stop > 0 && r == Q.stop && (i & 1) && (i / 2) >= max_bits) return;
+    extern __shared__ __align__(16) uint32_t smem[];
+    const Ctx x = setup(smem, tws);
+    const Prime &c = x.c;
+    const int half = 1 << r;
+    const bool upper = i >= half;
+    const uint32_t *ct = r == 0 ? Q.query : Q.v[r & 1] + (size_t)(upper ? i - half : i) * 4 * D;
+    const uint32_t *n1 = neg1 + ((size_t)r * 2 + x.g) * D;
+    const uint32_t tau = (uint32_t)(D >> r) + 1;
+    const uint32_t *row0 = ct + x.g * D, *row1 = ct + (2 + x.g) * D;
+
+    // tau(row0) in NTT form -> raw
+    uint64_t raw[VPT];
+    {
+        uint32_t v[VPT];
+#pragma unroll
+        for (int j = 0; j < VPT; j++) {
+            const int zs = auto_slot(VPT * x.t + j, tau);
+            uint32_t a = row0[zs];
+            v[j] = upper ? mont_mul(a, n1[zs], c.p, c.pinv) : a;   // (0, 2p)
+        }
+        ntt_inv(v, tw_inv(x), x.buf, c, x.t, x.bar);
+        exchange_icrt(x, v, raw);
+    }
+    const bool left = (r != 0) && !(i & 1);
+    const int tk = left ? sp.t_left : sp.t_right;
+    const uint32_t *W = (left ? Q.left : Q.right) + (size_t)r * 2 * tk * 2 * D;
+    const int bits = bits_per(tk);
+    const uint64_t mask = (1ull << bits) - 1;
+    uint32_t acc0[VPT], acc1[VPT];
+#pragma unroll
+    for (int j = 0; j < VPT; j++) acc0[j] = acc1[j] = 0;
+    for (int k = 0; k < tk; k++) {
+        uint32_t d[VPT];
+        digits(d, raw, bits * k, mask);
+        ntt_fwd(d, tw_fwd(x), x.buf, c, x.t, x.bar);
+        mac16(acc0, d, W + ((size_t)(0 * tk + k) * 2 + x.g) * D + VPT * x.t, c);
+        mac16(acc1, d, W + ((size_t)(1 * tk + k) * 2 + x.g) * D + VPT * x.t, c);
+    }
+    // v + acc (+ tau(row1) on row 1)
+    uint32_t o0[VPT], o1[VPT];
+    {
+        uint32_t b0[VPT], b1[VPT];
+        ld16(b0, row0 + VPT * x.t);
+        ld16(b1, row1 + VPT * x.t);
+        uint32_t nn[VPT];
+        if (upper) ld16(nn, n1 + VPT * x.t);
+#pragma unroll
+        for (int j = 0; j < VPT; j++) {
+            const int zs = auto_slot(VPT * x.t + j, tau);
+            uint32_t tb = row1[zs];
+            if (upper) {
+                tb = reduce2(mont_mul(tb, n1[zs], c.p, c.pinv), c.p);
+                b0[j] = reduce2(mont_mul(b0[j], nn[j], c.p, c.pinv), c.p);
+                b1[j] = reduce2(mont_mul(b1[j], nn[j], c.p, c.pinv), c.p);
+            }
+            o0[j] = canon4(b0[j] + acc0[j], c.p);
+            o1[j] = canon4(canon4(b1[j] + acc1[j], c.p) + tb, c.p);
+        }
+    }
+    const int zb = VPT * x.t;
+    if (r + 1 < Q.g) {
+        uint32_t *out = Q.v[(r + 1) & 1] + (size_t)i * 4 * D;
+        st16(out + x.g * D + zb, o0);
+        st16(out + (2 + x.g) * D + zb, o1);
+    }
+    if (r == Q.capture && (i & 1) && (i / 2) < max_bits) {
+        uint32_t *out = Q.gsw_in + (size_t)(i / 2) * 4 * D;
+        st16(out + x.g * D + zb, o0);
+        st16(out + (2 + x.g) * D + zb, o1);
+    }
+    if (r == Q.g - 1 && !(i & 1) && (i / 2) < (1 << Q.nu1)) {
+        uint32_t *s = Q.sel + (size_t)(i / 2) * D * 4;
+#pragma unroll
+        for (int j = 0; j < VPT; j++) {
+            s[(zb + j) * 4 + x.g] = o0[j];
+            s[(zb + j) * 4 + 2 + x.g] = o1[j];
+        }
+    }
+}
+
+cudaError_t launch_expand_round(const QDesc *qd, int nq, int r, int max_out, const StageParams &sp,
+                                const TwiddleSet *tw, const uint32_t *neg1, cudaStream_t st) {
+    cudaError_t e = cudaFuncSetAttribute(k_expand_round, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    k_expand_round<<<dim3(max_out, nq), THREADS, SMEM_BYTES, st>>>(qd, r, sp, tw, neg1);
+    return cudaGetLastError();
+}
+
+// --------------------------------------------- DB-multiply output to raw
+__global__ void __launch_bounds__(THREADS) k_acc_to_raw(const QDesc *__restrict__ qd, StageParams sp,
+                                                       const TwiddleSet *__restrict__ tws) {
+    const QDesc &Q = qd[blockIdx.y];
+    const int item = blockIdx.x;
+    if (!Q.active || item >= sp.T * (2 << Q.nu2)) return;
+    extern __shared__ __align__(16) uint32_t smem[];
+    const Ctx x = setup(smem, tws);
+    uint32_t v[VPT];
+    ld16(v, Q.acc + ((size_t)item * 2 + x.g) * D + VPT * x.t);
+    ntt_inv(v, tw_inv(x), x.buf, x.c, x.t, x.bar);
+    uint64_t raw[VPT];
+    exchange_icrt(x, v, raw);
+    uint64_t *o = Q.raw + (size_t)item * D;
+#pragma unroll
+    for (int j = 0; j < VPT; j++)
+        if ((j >> 3) == x.g) o[x.t + GROUP * j] = raw[j];
+}
+
+cudaError_t launch_acc_to_raw(const QDesc *qd, int nq, int max_items, const StageParams &sp,
+                              const TwiddleSet *tw, cudaStream_t st) {
+    cudaError_t e = cudaFuncSetAttribute(k_acc_to_raw, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    k_acc_to_raw<<<dim3(max_items, nq), THREADS, SMEM_BYTES, st>>>(qd, sp, tw);
+    return cudaGetLastError();
+}
+
+__global__ void k_sel_import(const uint64_t *__restrict__ in, uint32_t *__restrict__ sel, uint64_t total) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const int z = (int)(i % D);
+        const uint64_t rk = i / D;            // row*4 + (ct_row*2 + prime)
+        const int comp = (int)(rk % 4);
+        const uint64_t row = rk / 4;
+        sel[(row * D + z) * 4 + comp] = (uint32_t)in[i];
+    }
+}
+
+cudaError_t launch_sel_import(const uint64_t *in, uint32_t *sel, int rows, cudaStream_t st) {
+    const uint64_t total = (uint64_t)rows * 4 * D;
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > 8192) blocks = 8192;
+    k_sel_import<<<blocks, 256, 0, st>>>(in, sel, total);
+    return cudaGetLastError();
+}
+
+// -------------------------------------------------------- Regev -> GSW
+// Item blockIdx.x = dim*t_gsw + j: GSW column 2j+1 = the Regev encoding,
+// column 2j = V * NTT(G^-1_{2,t_conv}(raw(c))).  Output in Montgomery form
+// (the fold multiplies by it).
+__global__ void __launch_bounds__(THREADS) k_regev_to_gsw(const QDesc *__restrict__ qd, StageParams sp,
+                                                         const TwiddleSet *__restrict__ tws) {
+    const QDesc &Q = qd[blockIdx.y];
+    const int idx = blockIdx.x;
+    if (!Q.active || idx >= Q.nu2 * sp.t_gsw) return;
+    extern __shared__ __align__(16) uint32_t smem[];
+    const Ctx x = setup(smem, tws);
+    const Prime &c = x.c;
+    const int dim = idx / sp.t_gsw, jj = idx % sp.t_gsw;
+    const int cols = 2 * sp.t_gsw;
+    const uint32_t *ct = Q.gsw_in + (size_t)idx * 4 * D;
+    uint32_t *G = Q.gsw + (size_t)dim * 2 * cols * 2 * D;
+    const int bits = bits_per(sp.t_conv);
+    const uint64_t mask = (1ull << bits) - 1;
+    const int kc = 2 * sp.t_conv;
+    uint32_t acc0[VPT], acc1[VPT];
+#pragma unroll
+    for (int j = 0; j < VPT; j++) acc0[j] = acc1[j] = 0;
+    for (int row = 0; row < 2; row++) {
+        uint64_t raw[VPT];
+        {
+            uint32_t v[VPT];
+            ld16(v, ct + (row * 2 + x.g) * D + VPT * x.t);
+            ntt_inv(v, tw_inv(x), x.buf, c, x.t, x.bar);
+            exchange_icrt(x, v, raw);
+        }
+        for (int k = 0; k < sp.t_conv; k++) {
+            uint32_t d[VPT];
+            digits(d, raw, bits * k, mask);
+            ntt_fwd(d, tw_fwd(x), x.buf, c, x.t, x.bar);
+            const int col = row + 2 * k;
+            mac16(acc0, d, Q.conv + ((size_t)(0 * kc + col) * 2 + x.g) * D + VPT * x.t, c);
+            mac16(acc1, d, Q.conv + ((size_t)(1 * kc + col) * 2 + x.g) * D + VPT * x.t, c);
+        }
+    }
+    const int zb = VPT * x.t;
+    uint32_t o[VPT];
+#pragma unroll
+    for (int j = 0; j < VPT; j++) o[j] = to_mont(reduce2(acc0[j], c.p), c);
+    st16(G + ((size_t)(0 * cols + 2 * jj) * 2 + x.g) * D + zb, o);
+#pragma unroll
+    for (int j = 0; j < VPT; j++) o[j] = to_mont(reduce2(acc1[j], c.p), c);
+    st16(G + ((size_t)(1 * cols + 2 * jj) * 2 + x.g) * D + zb, o);
+    for (int row = 0; row < 2; row++) {
+        ld16(o, ct + (row * 2 + x.g) * D + zb);
+#pragma unroll
+        for (int j = 0; j < VPT; j++) o[j] = to_mont(o[j], c);
+        st16(G + ((size_t)(row * cols + 2 * jj + 1) * 2 + x.g) * D + zb, o);
+    }
+}
+
+cudaError_t launch_regev_to_gsw(const QDesc *qd, int nq, int max_items, const StageParams &sp,
+                                const TwiddleSet *tw, cudaStream_t st) {
+    cudaError_t e = cudaFuncSetAttribute(k_regev_to_gsw, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    k_regev_to_gsw<<<dim3(max_items, nq), THREADS, SMEM_BYTES, st>>>(qd, sp, tw);
+    return cudaGetLastError();
+}
+
+// G - C (the NTT of the constant 2^(b k) is that constant in every slot).
+__global__ void k_gsw_neg(const uint32_t *__restrict__ gsw, uint32_t *__restrict__ neg, uint64_t total, int t) {
+    const int cols = 2 * t;
+    const int bits = bits_per(t);
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t r = i / D;
+        const int k = (int)(r % 2); r /= 2;
+        const int col = (int)(r % cols); r /= cols;
+        const int row = (int)(r % 2);
+        const Prime c = prime_of(k);
+        uint32_t gval = 0;
+        if ((col & 1) == row && bits * (col / 2) < 64) gval = (uint32_t)((1ull << (bits * (col / 2))) % c.p);
+        uint32_t v = gval + c.p - gsw[i];
+        neg[i] = v >= c.p ? v - c.p : v;
+    }
+}
+
+cudaError_t launch_gsw_neg(const uint32_t *gsw, uint32_t *neg, int count, int t, cudaStream_t st) {
+    const uint64_t total = (uint64_t)count * 2 * 2 * t * 2 * D;
+    int blocks = (int)((total + 255) / 256);
+    if (blocks > 8192) blocks = 8192;
+    k_gsw_neg<<<blocks, 256, 0, st>>>(gsw, neg, total, t);
+    return cudaGetLastError();
+}
+
+// ----------------------------------------------------------------- fold
+// Level `level`: v[i] <- v[i] + C * NTT(G^-1(v[num_per+i]) - G^-1(v[i])),
+// which equals C*G^-1(v[num_per+i]) + (G - C)*G^-1(v[i]) exactly
+// (G*G^-1(x) = x for the unsigned digits), the fold of
+// gpu-pir/folding.cuh:9-27 with one product instead of two.
+__global__ void __launch_bounds__(THREADS) k_fold_level(const QDesc *__restrict__ qd, int level, StageParams sp,
+                                                       const TwiddleSet *__restrict__ tws) {
+    const QDesc &Q = qd[blockIdx.y];
+    if (!Q.active || level >= Q.nu2) return;
+    const int num_per = 1 << (Q.nu2 - 1 - level);
+    const int inst = blockIdx.x / num_per, i = blockIdx.x % num_per;
+    if (inst >= sp.T) return;
+    extern __shared__ __align__(16) uint32_t smem[];
+    const Ctx x = setup(smem, tws);
+    const Prime &c = x.c;
+    const int cols = 1 << Q.nu2;
+    uint64_t *base = Q.raw + (size_t)inst * cols * 2 * D;
+    uint64_t *v0 = base + (size_t)i * 2 * D;
+    const uint64_t *v1 = base + (size_t)(num_per + i) * 2 * D;
+    const int tg = sp.t_gsw, gc = 2 * tg;
+    const uint32_t *C = Q.gsw + (size_t)(Q.nu2 - 1 - level) * 2 * gc * 2 * D;
+    const int bits = bits_per(tg);
+    const uint64_t mask = (1ull << bits) - 1;
+    uint32_t acc0[VPT], acc1[VPT];
+#pragma unroll
+    for (int j = 0; j < VPT; j++) acc0[j] = acc1[j] = 0;
+    for (int row = 0; row < 2; row++) {
+        for (int k = 0; k < tg; k++) {
+            const int sh = bits * k;
+            uint32_t d[VPT];
+#pragma unroll
+            for (int j = 0; j < VPT; j++) {
+                const int e = x.t + GROUP * j;
+                const uint32_t a = (uint32_t)((__ldg(v1 + row * D + e) >> sh) & mask);
+                const uint32_t b = (uint32_t)((v0[row * D + e] >> sh) & mask);
+                d[j] = a >= b ? a - b : a + c.p - b;
+            }
+            ntt_fwd(d, tw_fwd(x), x.buf, c, x.t, x.bar);
+            const int col = row + 2 * k;
+            mac16(acc0, d, C + ((size_t)(0 * gc + col) * 2 + x.g) * D + VPT * x.t, c);
+            mac16(acc1, d, C + ((size_t)(1 * gc + col) * 2 + x.g) * D + VPT * x.t, c);
+        }
+    }
+    ntt_inv(acc0, tw_inv(x), x.buf, c, x.t, x.bar);
+    ntt_inv(acc1, tw_inv(x), x.buf, c, x.t, x.bar);
+    group_sync(x.bar);  // this group's last transpose reads are done
+    uint32_t *ex0 = x.bufs + x.g * 2 * D, *ex1 = ex0 + D;   // [row][prime] = bufs + (prime*2 + row)*D
+#pragma unroll
+    for (int j = 0; j < VPT; j++) {
+        ex0[x.t + GROUP * j] = acc0[j];
+        ex1[x.t + GROUP * j] = acc1[j];
+    }
+    __syncthreads();
+    // group g finishes row g
+    const int row = x.g;
+    const uint32_t *a0 = x.bufs + row * D, *a1 = x.bufs + 2 * D + row * D;
+#pragma unroll
+    for (int j = 0; j < VPT; j++) {
+        const int e = x.t + GROUP * j;
+        uint64_t y = icrt(a0[e], a1[e]) + v0[row * D + e];
+        v0[row * D + e] = y >= QQ ? y - QQ : y;
+    }
+}
+
+cudaError_t launch_fold_level(const QDesc *qd, int nq, int level, int max_items, const StageParams &sp,
+                              const TwiddleSet *tw, cudaStream_t st) {
+    cudaError_t e = cudaFuncSetAttribute(k_fold_level, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    k_fold_level<<<dim3(max_items, nq), THREADS, SMEM_BYTES, st>>>(qd, level, sp, tw);
+    return cudaGetLastError();
+}
+
+// ----------------------------------------------------------------- pack
+__device__ __forceinline__ uint32_t rescale_q(uint64_t x, int bits_out) {
+    // round(x * 2^bits_out / q) mod 2^bits_out, x read as centred in Z_q
+    const uint64_t mask = (1ull << bits_out) - 1;
+    const bool neg = x >= (QQ + 1) / 2;
+    const uint64_t a = neg ? QQ - x : x;
+    const unsigned __int128 num = ((unsigned __int128)a << bits_out) + QQ / 2;
+    const uint64_t y = (uint64_t)(num / QQ) & mask;
+    return (uint32_t)(neg ? ((0 - y) & mask) : y);
+}
+
+constexpr int PACK_MAX_N = 2;
+
+// Column c = blockIdx.x of query blockIdx.y: sum over r < n of
+// W_r * NTT(G^-1(ct[r*n+c].row0)) + e_{1+r} * NTT(ct[r*n+c].row1), then raw,
+// then row 0 rescaled to 2^q2_bits and rows 1..n to 4p.
+__global__ void __launch_bounds__(THREADS) k_pack(const QDesc *__restrict__ qd, StageParams sp,
+                                                 const TwiddleSet *__restrict__ tws) {
+    const QDesc &Q = qd[blockIdx.y];
+    const int col = blockIdx.x;
+    if (!Q.active || col >= sp.n) return;
+    extern __shared__ __align__(16) uint32_t smem[];
+    const Ctx x = setup(smem, tws);
+    const Prime &c = x.c;
+    const int n = sp.n, tcv = sp.t_conv;
+    const int cols = 1 << Q.nu2;
+    const int bits = bits_per(tcv);
+    const uint64_t mask = (1ull << bits) - 1;
+    uint32_t acc[PACK_MAX_N + 1][VPT];
+#pragma unroll
+    for (int a = 0; a <= PACK_MAX_N; a++)
+#pragma unroll
+        for (int j = 0; j < VPT; j++) acc[a][j] = 0;
+    for (int r = 0; r < n; r++) {
+        const uint64_t *ct = Q.raw + (size_t)(r * n + col) * cols * 2 * D;   // folded result of instance r*n+col
+        const uint32_t *W = Q.pack + (size_t)r * (n + 1) * tcv * 2 * D;
+        uint64_t raw[VPT];
+#pragma unroll
+        for (int j = 0; j < VPT; j++) raw[j] = ct[x.t + GROUP * j];
+        for (int k = 0; k < tcv; k++) {
+            uint32_t d[VPT];
+            digits(d, raw, bits * k, mask);
+            ntt_fwd(d, tw_fwd(x), x.buf, c, x.t, x.bar);
+#pragma unroll
+            for (int a = 0; a <= PACK_MAX_N; a++)
+                if (a <= n) mac16(acc[a], d, W + ((size_t)(a * tcv + k) * 2 + x.g) * D + VPT * x.t, c);
+        }
+        uint32_t b[VPT];
+#pragma unroll
+        for (int j = 0; j < VPT; j++) b[j] = mod_u64(ct[D + x.t + GROUP * j], c);
+        ntt_fwd(b, tw_fwd(x), x.buf, c, x.t, x.bar);
+#pragma unroll
+        for (int a = 1; a <= PACK_MAX_N; a++)
+            if (a == 1 + r) {
+#pragma unroll
+                for (int j = 0; j < VPT; j++) acc[a][j] = reduce2(acc[a][j] + reduce2(b[j], 2 * c.p), 2 * c.p);
+            }
+    }
+#pragma unroll
+    for (int a = 0; a <= PACK_MAX_N; a++) {
+        if (a > n) break;
+        ntt_inv(acc[a], tw_inv(x), x.buf, c, x.t, x.bar);
+        uint64_t raw[VPT];
+        exchange_icrt(x, acc[a], raw);
+        const int ob = a == 0 ? sp.q2_bits : sp.pt_bits + 2;
+        uint32_t *o = Q.ms + ((size_t)a * n + col) * D;
+        if (x.g == 0) {
+#pragma unroll
+            for (int j = 0; j < VPT; j++) o[x.t + GROUP * j] = rescale_q(raw[j], ob);
+        }
+    }
+}
+
+cudaError_t launch_pack(const QDesc *qd, int nq, const StageParams &sp, const TwiddleSet *tw, cudaStream_t st) {
+    if (sp.n > PACK_MAX_N) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(k_pack, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    if (e != cudaSuccess) return e;
+    k_pack<<<dim3(sp.n, nq), THREADS, SMEM_BYTES, st>>>(qd, sp, tw);
+    return cudaGetLastError();
+}
+
+uint64_t response_bytes(const StageParams &sp) {
+    const uint64_t bits = (uint64_t)sp.n * D * sp.q2_bits + (uint64_t)sp.n * sp.n * D * (sp.pt_bits + 2);
+    return (bits + 63) / 64 * 8;
+}
+
+// Serialise: first n*D values of q2_bits, then n*n*D values of pt_bits+2,
+// least significant bit first, packed into little-endian 32-bit words.
+__global__ void k_bitpack(const QDesc *__restrict__ qd, StageParams sp, uint64_t words) {
+    const QDesc &Q = qd[blockIdx.y];
+    if (!Q.active) return;
+    const uint64_t n0 = (uint64_t)sp.n * D;
+    const uint64_t n1 = (uint64_t)sp.n * sp.n * D;
+    const int b0 = sp.q2_bits, b1 = sp.pt_bits + 2;
+    const uint64_t end0 = n0 * b0;
+    uint32_t *out = reinterpret_cast<uint32_t *>(Q.resp);
+    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < words; w += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t lo = w * 32, hi = lo + 32;
+        uint64_t acc = 0;
+        // section 0
+        if (lo < end0) {
+            uint64_t e = lo / b0;
+            for (; e < n0 && e * b0 < hi; e++) {
+                const int64_t off = (int64_t)(e * b0) - (int64_t)lo;
+                const uint64_t v = Q.ms[e];
+                acc |= off >= 0 ? (v << off) : (v >> (-off));
+            }
+        }
+        if (hi > end0) {
+            uint64_t e = lo > end0 ? (lo - end0) / b1 : 0;
+            for (; e < n1 && end0 + e * b1 < hi; e++) {
+                const int64_t off = (int64_t)(end0 + e * b1) - (int64_t)lo;
+                const uint64_t v = Q.ms[n0 + e];
+                acc |= off >= 0 ? (v << off) : (v >> (-off));
+            }
+        }
+        out[w] = (uint32_t)acc;
+    }
+}
+
+cudaError_t launch_bitpack(const QDesc *qd, int nq, const StageParams &sp, uint64_t resp_bytes, cudaStream_t st) {
+    const uint64_t words = resp_bytes / 4;
+    int blocks = (int)((words + 255) / 256);
+    k_bitpack<<<dim3(blocks, nq), 256, 0, st>>>(qd, sp, words);
+    return cudaGetLastError();
+}
+
+}  // namespace sp

@@ -1,0 +1,39 @@
+// Per-query descriptors and launchers of the query-dependent stages:
+// coefficient expansion (R6, R7, R8), Regev->GSW conversion (R9), G - C
+// (R10), DB-multiply output to raw (R13), folding (R12) and packing /
+// modulus switching / serialisation (R14).
+//
+// Every kernel takes an array of QDesc (one per query of the launch) so that
+// queries against databases of different shapes run in the same launch.
+#pragma once
+#include "kernels.cuh"
+
+namespace sp {
+
+// u64 canonical residues [count][2][D] -> u32 (optionally Montgomery form)
+cudaError_t launch_narrow(const uint64_t *in, uint32_t *out, uint64_t planes, bool to_mont, cudaStream_t st);
+// u32 [count][2][D] (optionally from Montgomery form) -> u64 canonical
+cudaError_t launch_widen(const uint32_t *in, uint64_t *out, uint64_t planes, bool from_mont, cudaStream_t st);
+
+// DB-multiply output (NTT form) -> raw fold input, every query of qd
+cudaError_t launch_acc_to_raw(const QDesc *qd, int nq, int max_items, const StageParams &sp,
+                              const TwiddleSet *tw, cudaStream_t st);
+// selectors u64 [rows][2 rows][2][D] -> device selector layout u32 [rows][D][4]
+cudaError_t launch_sel_import(const uint64_t *in, uint32_t *sel, int rows, cudaStream_t st);
+
+cudaError_t launch_expand_round(const QDesc *qd, int nq, int r, int max_out, const StageParams &sp,
+                                const TwiddleSet *tw, const uint32_t *neg1, cudaStream_t st);
+cudaError_t launch_regev_to_gsw(const QDesc *qd, int nq, int max_items, const StageParams &sp,
+                                const TwiddleSet *tw, cudaStream_t st);
+// G - C for count GSW ciphertexts (canonical in and out)
+cudaError_t launch_gsw_neg(const uint32_t *gsw, uint32_t *neg, int count, int t, cudaStream_t st);
+cudaError_t launch_fold_level(const QDesc *qd, int nq, int level, int max_items, const StageParams &sp,
+                              const TwiddleSet *tw, cudaStream_t st);
+cudaError_t launch_pack(const QDesc *qd, int nq, const StageParams &sp, const TwiddleSet *tw,
+                        cudaStream_t st);
+cudaError_t launch_bitpack(const QDesc *qd, int nq, const StageParams &sp, uint64_t resp_bytes,
+                           cudaStream_t st);
+
+uint64_t response_bytes(const StageParams &sp);
+
+}  // namespace sp

@@ -1,0 +1,1049 @@
+// C ABI of the Spiral answer path (include/spiralpir.h): context, device
+// memory under an HBM budget, databases, client keys, the answer pipeline
+// and the stage entry points used by the parity tests.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/spiralpir.h"
+#include "answer.cuh"
+
+using namespace sp;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+#define CU(call)                                                                                   \
+    do {                                                                                           \
+        cudaError_t e_ = (call);                                                                   \
+        if (e_ != cudaSuccess)                                                                     \
+            return fail(e_ == cudaErrorMemoryAllocation ? SP_ERR_NOMEM : SP_ERR_CUDA,              \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                       \
+    } while (0)
+
+int ceil_log2(uint64_t x) {
+    int v = 0;
+    uint64_t p = 1;
+    while (p < x) { p <<= 1; v++; }
+    return v;
+}
+
+struct Db {
+    DbLayout L{};
+    uint64_t *d = nullptr;
+    uint64_t bytes = 0;
+};
+
+struct Client {
+    int n_left = 0, n_right = 0;
+    uint32_t *keys = nullptr;   // one allocation: left | right | conv | pack
+    const uint32_t *left = nullptr, *right = nullptr, *conv = nullptr, *pack = nullptr;
+    uint64_t bytes = 0;
+    uint64_t stamp = 0;         // last use (LRU)
+};
+
+struct Shape {
+    int nu1 = 0, nu2 = 0, g = 0;
+};
+
+// Workspace of one query slot, sized for a maximal shape.
+struct Slot {
+    uint8_t *base = nullptr;
+    uint64_t bytes = 0;
+    QDesc q{};
+    uint32_t *query32 = nullptr;
+    uint64_t *query64 = nullptr;
+    int client = -1, db = -1;
+};
+
+}  // namespace
+
+struct sp_ctx {
+    sp_params p{};
+    StageParams sp{};
+    int device = 0;
+    cudaStream_t st = nullptr;
+    TwiddleSet *d_tw = nullptr;
+    uint32_t *d_neg1 = nullptr;     // [11][2][D] Montgomery form of NTT(x^(-2^r))
+    int *d_err = nullptr;
+    QDesc *d_qd = nullptr;          // [max_batch]
+    QDesc *h_qd = nullptr;          // pinned mirror
+    uint8_t *h_stage = nullptr;     // pinned staging for queries/responses
+    uint64_t stage_bytes = 0;
+    std::map<int, Db> dbs;
+    std::map<int, Client> clients;
+    std::vector<Slot> slots;
+    Shape slot_shape{};
+    uint64_t budget = 0, used = 0;
+    uint64_t clock = 0;
+    std::mutex mu;
+    cudaEvent_t ev[6]{};
+    sp_stats_out stats{};
+    int staged = 0;
+};
+
+namespace {
+
+int alloc(sp_ctx *c, void **p, uint64_t bytes) {
+    if (c->budget && c->used + bytes > c->budget)
+        return fail(SP_ERR_NOMEM, "HBM budget exceeded: need " + std::to_string(bytes) + " more bytes, " +
+                                      std::to_string(c->budget - c->used) + " left");
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return fail(SP_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    c->used += bytes;
+    return SP_OK;
+}
+
+void release(sp_ctx *c, void *p, uint64_t bytes) {
+    if (p) {
+        cudaFree(p);
+        c->used -= bytes;
+    }
+}
+
+int check_params(const sp_params *p) {
+    if (!p) return fail(SP_ERR_INVALID, "params is NULL");
+    if (p->n < 1 || p->n > 2) return fail(SP_ERR_UNSUPPORTED, "n must be 1 or 2");
+    if (p->pt_bits < 1 || p->pt_bits > 8) return fail(SP_ERR_UNSUPPORTED, "pt_bits must be in [1, 8]");
+    for (int t : {p->t_exp_left, p->t_exp_right, p->t_gsw, p->t_conv})
+        if (t < 3 || t > 56) return fail(SP_ERR_UNSUPPORTED, "gadget lengths must be in [3, 56]");
+    if (p->q2_bits < p->pt_bits + 2 || p->q2_bits > 32)
+        return fail(SP_ERR_INVALID, "q2_bits must be in [pt_bits+2, 32]");
+    if (p->max_batch < 1 || p->max_batch > 4096) return fail(SP_ERR_INVALID, "max_batch must be in [1, 4096]");
+    return SP_OK;
+}
+
+Shape shape_of(const sp_ctx *c, int nu1, int nu2) {
+    Shape s;
+    s.nu1 = nu1;
+    s.nu2 = nu2;
+    s.g = ceil_log2((uint64_t)c->sp.t_gsw * nu2 + (1ull << nu1));
+    return s;
+}
+
+uint64_t slot_bytes(const sp_ctx *c, const Shape &s) {
+    const uint64_t ct = 4ull * D * 4;   // NTT ciphertext bytes
+    const int T = c->sp.T;
+    uint64_t b = 0;
+    auto add = [&](uint64_t x) { b += (x + 255) & ~255ull; };
+    add(ct);                                  // query32
+    add(ct * 2);                              // query64
+    add(ct << s.g);                           // v[0]
+    add(ct << s.g);                           // v[1]
+    add((uint64_t)D * 16 << s.nu1);           // sel
+    add(ct * s.nu2 * c->sp.t_gsw);            // gsw_in
+    add((uint64_t)s.nu2 * 2 * 2 * c->sp.t_gsw * 2 * D * 4);   // gsw
+    add(((uint64_t)T * ct) << s.nu2);         // acc
+    add(((uint64_t)T * 2 * D * 8) << s.nu2);  // raw
+    add((uint64_t)(c->sp.n + 1) * c->sp.n * D * 4);           // ms
+    add(response_bytes(c->sp));               // resp
+    return b;
+}
+
+void carve(sp_ctx *c, Slot &sl, const Shape &s) {
+    uint8_t *p = sl.base;
+    const uint64_t ct = 4ull * D * 4;
+    const int T = c->sp.T;
+    auto take = [&](uint64_t x) {
+        uint8_t *r = p;
+        p += (x + 255) & ~255ull;
+        return r;
+    };
+    sl.query32 = (uint32_t *)take(ct);
+    sl.query64 = (uint64_t *)take(ct * 2);
+    QDesc &q = sl.q;
+    q = QDesc{};
+    q.query = sl.query32;
+    q.v[0] = (uint32_t *)take(ct << s.g);
+    q.v[1] = (uint32_t *)take(ct << s.g);
+    q.sel = (uint32_t *)take((uint64_t)D * 16 << s.nu1);
+    q.gsw_in = (uint32_t *)take(ct * s.nu2 * c->sp.t_gsw);
+    q.gsw = (uint32_t *)take((uint64_t)s.nu2 * 2 * 2 * c->sp.t_gsw * 2 * D * 4);
+    q.acc = (uint32_t *)take(((uint64_t)T * ct) << s.nu2);
+    q.raw = (uint64_t *)take(((uint64_t)T * 2 * D * 8) << s.nu2);
+    q.ms = (uint32_t *)take((uint64_t)(c->sp.n + 1) * c->sp.n * D * 4);
+    q.resp = take(response_bytes(c->sp));
+}
+
+// Make sure there are `count` slots big enough for shape `need`.
+int ensure_slots(sp_ctx *c, const Shape &need, int count) {
+    Shape s = c->slot_shape;
+    bool grow = need.nu1 > s.nu1 || need.nu2 > s.nu2 || need.g > s.g;
+    s.nu1 = std::max(s.nu1, need.nu1);
+    s.nu2 = std::max(s.nu2, need.nu2);
+    s.g = std::max(s.g, need.g);
+    if (grow) {
+        CU(cudaStreamSynchronize(c->st));
+        for (auto &sl : c->slots) release(c, sl.base, sl.bytes);
+        c->slots.clear();
+        c->staged = 0;
+    }
+    c->slot_shape = s;
+    const uint64_t b = slot_bytes(c, s);
+    while ((int)c->slots.size() < count) {
+        Slot sl;
+        int rc = alloc(c, (void **)&sl.base, b);
+        if (rc) return rc;
+        sl.bytes = b;
+        carve(c, sl, s);
+        c->slots.push_back(sl);
+    }
+    return SP_OK;
+}
+
+int ensure_staging(sp_ctx *c, uint64_t bytes) {
+    if (c->stage_bytes >= bytes) return SP_OK;
+    if (c->h_stage) cudaFreeHost(c->h_stage);
+    c->h_stage = nullptr;
+    CU(cudaMallocHost(&c->h_stage, bytes));
+    c->stage_bytes = bytes;
+    return SP_OK;
+}
+
+void fill_desc(sp_ctx *c, QDesc &q, const Client &cl, const Db &db) {
+    q.left = cl.left;
+    q.right = cl.right;
+    q.conv = cl.conv;
+    q.pack = cl.pack;
+    q.nu1 = db.L.nu1;
+    q.nu2 = db.L.nu2;
+    Shape s = shape_of(c, q.nu1, q.nu2);
+    q.g = s.g;
+    q.stop = ceil_log2((uint64_t)c->sp.t_gsw * q.nu2);
+    q.capture = (q.stop > 0 && q.stop < q.g) ? q.stop : q.g - 1;
+    q.active = 1;
+}
+
+int check_client_for(const sp_ctx *c, const Client &cl, const Db &db, int *need_left, int *need_right) {
+    Shape s = shape_of(c, db.L.nu1, db.L.nu2);
+    int stop = ceil_log2((uint64_t)c->sp.t_gsw * db.L.nu2);
+    *need_left = s.g;
+    *need_right = std::min(stop, s.g - 1) + 1;
+    if (cl.n_left < *need_left || cl.n_right < *need_right)
+        return fail(SP_ERR_INVALID, "client keys do not cover this database shape (need " +
+                                        std::to_string(*need_left) + " left / " + std::to_string(*need_right) +
+                                        " right expansion keys)");
+    return SP_OK;
+}
+
+// Run the answer pipeline for queries in slots [0, nq) (descriptors already
+// in c->h_qd / c->d_qd, queries in slot.query32).  Records stage events.
+int run_pipeline(sp_ctx *c, int nq, const std::vector<int> &db_of_slot) {
+    cudaStream_t st = c->st;
+    const StageParams &sp = c->sp;
+    int max_g = 0, max_nu2 = 0, max_items = 0;
+    for (int i = 0; i < nq; i++) {
+        max_g = std::max(max_g, c->h_qd[i].g);
+        max_nu2 = std::max(max_nu2, c->h_qd[i].nu2);
+        max_items = std::max(max_items, c->h_qd[i].nu2 * sp.t_gsw);
+    }
+    uint64_t launches = 0;
+    CU(cudaEventRecord(c->ev[0], st));
+    for (int r = 0; r < max_g; r++) {
+        CU(launch_expand_round(c->d_qd, nq, r, 2 << r, sp, c->d_tw, c->d_neg1, st));
+        launches++;
+    }
+    CU(cudaEventRecord(c->ev[1], st));
+    CU(launch_regev_to_gsw(c->d_qd, nq, max_items, sp, c->d_tw, st));
+    launches++;
+    CU(cudaEventRecord(c->ev[2], st));
+    // first-dimension multiply: consecutive slots of the same database share a launch
+    uint64_t mul_bytes = 0, mul_calls = 0;
+    for (int i = 0; i < nq;) {
+        int j = i;
+        while (j < nq && db_of_slot[j] == db_of_slot[i]) j++;
+        const Db &db = c->dbs.at(db_of_slot[i]);
+        CU(launch_db_mul(db.d, db.L, c->d_qd + i, j - i, c->d_err, st));
+        launches++;
+        mul_calls++;
+        mul_bytes += db.L.words * 8 + (uint64_t)(j - i) * ((uint64_t)db.L.rows * D * 16 +
+                                                          (uint64_t)db.L.T * db.L.cols * 4 * D * 4);
+        i = j;
+    }
+    CU(cudaEventRecord(c->ev[3], st));
+    CU(launch_acc_to_raw(c->d_qd, nq, sp.T * (2 << max_nu2), sp, c->d_tw, st));
+    launches++;
+    for (int lvl = 0; lvl < max_nu2; lvl++) {
+        CU(launch_fold_level(c->d_qd, nq, lvl, sp.T << (max_nu2 - 1 - lvl), sp, c->d_tw, st));
+        launches++;
+    }
+    CU(cudaEventRecord(c->ev[4], st));
+    CU(launch_pack(c->d_qd, nq, sp, c->d_tw, st));
+    CU(launch_bitpack(c->d_qd, nq, sp, response_bytes(sp), st));
+    launches += 2;
+    CU(cudaEventRecord(c->ev[5], st));
+    c->stats.launches += launches;
+    c->stats.db_mul_calls += mul_calls;
+    c->stats.db_mul_bytes += mul_bytes;
+    c->stats.answers += nq;
+    return SP_OK;
+}
+
+int collect_stats(sp_ctx *c) {
+    float ms[5], tot;
+    for (int i = 0; i < 5; i++) CU(cudaEventElapsedTime(&ms[i], c->ev[i], c->ev[i + 1]));
+    CU(cudaEventElapsedTime(&tot, c->ev[0], c->ev[5]));
+    c->stats.ms_expand += ms[0];
+    c->stats.ms_convert += ms[1];
+    c->stats.ms_db_mul += ms[2];
+    c->stats.ms_fold += ms[3];
+    c->stats.ms_pack += ms[4];
+    c->stats.ms_total += tot;
+    return SP_OK;
+}
+
+int check_device_err(sp_ctx *c) {
+    int h = 0;
+    CU(cudaMemcpyAsync(&h, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CU(cudaStreamSynchronize(c->st));
+    if (h) {
+        CU(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
+        return fail(SP_ERR_DEVICE, "a device-side bounded wait ran out (code " + std::to_string(h) + ")");
+    }
+    return SP_OK;
+}
+
+// Temporary device buffer for stage calls (freed on scope exit).
+struct Tmp {
+    sp_ctx *c;
+    void *p = nullptr;
+    uint64_t b = 0;
+    explicit Tmp(sp_ctx *ctx) : c(ctx) {}
+    int get(uint64_t bytes) {
+        b = bytes;
+        return alloc(c, &p, bytes ? bytes : 16);
+    }
+    ~Tmp() { release(c, p, b ? b : 16); }
+    template <typename T> T *as() const { return (T *)p; }
+};
+
+#define TRY(x)                 \
+    do {                       \
+        int rc_ = (x);         \
+        if (rc_) return rc_;   \
+    } while (0)
+
+}  // namespace
+
+// ===================================================================== API
+extern "C" {
+
+int sp_last_error(char *buf, size_t len) {
+    if (!buf || !len) return SP_ERR_INVALID;
+    snprintf(buf, len, "%s", g_err.c_str());
+    return SP_OK;
+}
+
+int sp_ctx_create(const sp_params *params, uint64_t hbm_budget_bytes, sp_ctx **out) {
+    if (!out) return fail(SP_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    TRY(check_params(params));
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(SP_ERR_CUDA, "no CUDA device");
+    }
+    sp_ctx *c = new sp_ctx();
+    c->p = *params;
+    c->sp.n = params->n;
+    c->sp.T = params->n * params->n;
+    c->sp.pt_bits = params->pt_bits;
+    c->sp.q2_bits = params->q2_bits;
+    c->sp.t_left = params->t_exp_left;
+    c->sp.t_right = params->t_exp_right;
+    c->sp.t_gsw = params->t_gsw;
+    c->sp.t_conv = params->t_conv;
+    c->budget = hbm_budget_bytes;
+    auto bail = [&](int rc) {
+        sp_ctx_destroy(c);
+        return rc;
+    };
+    if (cudaGetDevice(&c->device) != cudaSuccess) return bail(fail(SP_ERR_CUDA, "cudaGetDevice failed"));
+    if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(SP_ERR_CUDA, "cudaStreamCreate failed"));
+    for (auto &e : c->ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return bail(fail(SP_ERR_CUDA, "cudaEventCreate failed"));
+    int rc = alloc(c, (void **)&c->d_tw, sizeof(TwiddleSet));
+    if (!rc) rc = alloc(c, (void **)&c->d_neg1, (uint64_t)LOGD * 2 * D * 4);
+    if (!rc) rc = alloc(c, (void **)&c->d_err, 16);
+    if (!rc) rc = alloc(c, (void **)&c->d_qd, sizeof(QDesc) * params->max_batch);
+    if (rc) return bail(rc);
+    if (cudaMallocHost(&c->h_qd, sizeof(QDesc) * params->max_batch) != cudaSuccess)
+        return bail(fail(SP_ERR_NOMEM, "cudaMallocHost failed"));
+    memset(c->h_qd, 0, sizeof(QDesc) * params->max_batch);
+    // constant tables
+    std::vector<TwiddleSet> tw(1);
+    build_twiddles_host(tw.data());
+    std::vector<uint32_t> neg1((size_t)LOGD * 2 * D);
+    const uint32_t psi[2] = {66687u, 158221u};
+    for (int r = 0; r < LOGD; r++)
+        for (int k = 0; k < 2; k++) {
+            const Prime pr = prime_of(k);
+            const uint64_t p = pr.p;
+            const uint64_t psi_inv = powmod_c(psi[k], 4095, p);
+            for (int z = 0; z < D; z++) {
+                uint32_t rz = 0, x = z;
+                for (int b = 0; b < LOGD; b++) { rz = (rz << 1) | (x & 1); x >>= 1; }
+                // slot z of x^(-2^r): psi^(-(2*brev(z)+1) * 2^r)
+                uint64_t v = powmod_c(psi_inv, ((uint64_t)(2 * rz + 1) << r) % 4096, p);
+                neg1[((size_t)r * 2 + k) * D + z] = (uint32_t)(v * pr.two32 % p);
+            }
+        }
+    if (cudaMemcpy(c->d_tw, tw.data(), sizeof(TwiddleSet), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(c->d_neg1, neg1.data(), neg1.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(c->d_err, 0, 16) != cudaSuccess)
+        return bail(fail(SP_ERR_CUDA, "constant upload failed"));
+    *out = c;
+    return SP_OK;
+}
+
+int sp_ctx_destroy(sp_ctx *c) {
+    if (!c) return SP_OK;
+    if (c->st) cudaStreamSynchronize(c->st);
+    for (auto &kv : c->dbs) release(c, kv.second.d, kv.second.bytes);
+    for (auto &kv : c->clients) release(c, kv.second.keys, kv.second.bytes);
+    for (auto &sl : c->slots) release(c, sl.base, sl.bytes);
+    release(c, c->d_tw, sizeof(TwiddleSet));
+    release(c, c->d_neg1, (uint64_t)LOGD * 2 * D * 4);
+    release(c, c->d_err, 16);
+    release(c, c->d_qd, sizeof(QDesc) * c->p.max_batch);
+    if (c->h_qd) cudaFreeHost(c->h_qd);
+    if (c->h_stage) cudaFreeHost(c->h_stage);
+    for (auto &e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;
+    return SP_OK;
+}
+
+int sp_response_bytes(const sp_ctx *c, uint64_t *bytes) {
+    if (!c || !bytes) return fail(SP_ERR_INVALID, "NULL argument");
+    *bytes = response_bytes(c->sp);
+    return SP_OK;
+}
+
+int sp_hbm_used(const sp_ctx *c, uint64_t *bytes) {
+    if (!c || !bytes) return fail(SP_ERR_INVALID, "NULL argument");
+    *bytes = c->used;
+    return SP_OK;
+}
+
+// ------------------------------------------------------------- databases
+static int db_check_shape(sp_ctx *c, int nu1, int nu2) {
+    if (nu1 < 1 || nu1 > 14 || nu2 < 1 || nu2 > 14) return fail(SP_ERR_INVALID, "nu1/nu2 out of range");
+    if (shape_of(c, nu1, nu2).g > LOGD)
+        return fail(SP_ERR_UNSUPPORTED, "expansion needs more than 11 rounds (t_gsw*nu2 + 2^nu1 > 2048)");
+    DbLayout L = make_db_layout(c->sp.T, nu1, nu2);
+    const int tcg = L.T * L.cg;
+    if (tcg != 4 && tcg != 8 && tcg != 16)
+        return fail(SP_ERR_UNSUPPORTED, "database shape has fewer than 4 polynomials per tile row");
+    if (L.rows > 128 && L.rows % 128) return fail(SP_ERR_UNSUPPORTED, "rows must be a multiple of 128");
+    return SP_OK;
+}
+
+static int db_alloc(sp_ctx *c, int db_id, int nu1, int nu2, Db &db) {
+    TRY(db_check_shape(c, nu1, nu2));
+    if (c->dbs.count(db_id)) {
+        CU(cudaStreamSynchronize(c->st));
+        release(c, c->dbs[db_id].d, c->dbs[db_id].bytes);
+        c->dbs.erase(db_id);
+    }
+    db.L = make_db_layout(c->sp.T, nu1, nu2);
+    db.bytes = db.L.words * 8;
+    return alloc(c, (void **)&db.d, db.bytes);
+}
+
+int sp_db_load_plain(sp_ctx *c, int32_t db_id, const uint8_t *records, uint64_t n_records, int32_t nu1,
+                     int32_t nu2) {
+    if (!c || !records) return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (n_records != (1ull << (nu1 + nu2))) return fail(SP_ERR_INVALID, "n_records must be 2^(nu1+nu2)");
+    Db db;
+    TRY(db_alloc(c, db_id, nu1, nu2, db));
+    // stream the records through a pinned staging buffer in chunks
+    const uint64_t rec_bytes = (uint64_t)c->sp.T * D;
+    const uint64_t chunk_recs = std::max<uint64_t>(1, (64ull << 20) / rec_bytes);
+    Tmp dev(c);
+    int rc = dev.get(2 * chunk_recs * rec_bytes);
+    if (!rc) rc = ensure_staging(c, 2 * chunk_recs * rec_bytes);
+    if (rc) {
+        release(c, db.d, db.bytes);
+        return rc;
+    }
+    int buf = 0;
+    cudaEvent_t done[2];
+    cudaEventCreateWithFlags(&done[0], cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&done[1], cudaEventDisableTiming);
+    cudaEventRecord(done[0], c->st);
+    cudaEventRecord(done[1], c->st);
+    cudaError_t err = cudaSuccess;
+    for (uint64_t r0 = 0; r0 < n_records && err == cudaSuccess; r0 += chunk_recs, buf ^= 1) {
+        const uint64_t cnt = std::min(chunk_recs, n_records - r0);
+        uint8_t *hs = c->h_stage + buf * chunk_recs * rec_bytes;
+        uint8_t *ds = dev.as<uint8_t>() + buf * chunk_recs * rec_bytes;
+        cudaEventSynchronize(done[buf]);   // staging half free again
+        memcpy(hs, records + r0 * rec_bytes, cnt * rec_bytes);
+        err = cudaMemcpyAsync(ds, hs, cnt * rec_bytes, cudaMemcpyHostToDevice, c->st);
+        if (err == cudaSuccess) err = launch_db_encode(ds, r0, cnt, c->sp.pt_bits, db.L, db.d, c->d_tw, c->st);
+        cudaEventRecord(done[buf], c->st);
+    }
+    if (err == cudaSuccess) err = cudaStreamSynchronize(c->st);
+    cudaEventDestroy(done[0]);
+    cudaEventDestroy(done[1]);
+    if (err != cudaSuccess) {
+        release(c, db.d, db.bytes);
+        return fail(SP_ERR_CUDA, std::string("database encode: ") + cudaGetErrorString(err));
+    }
+    c->dbs[db_id] = db;
+    return SP_OK;
+}
+
+int sp_db_load_ntt(sp_ctx *c, int32_t db_id, const uint32_t *planes, int32_t nu1, int32_t nu2) {
+    if (!c || !planes) return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    Db db;
+    TRY(db_alloc(c, db_id, nu1, nu2, db));
+    Tmp dev(c);
+    int rc = dev.get(db.L.words * 8);
+    if (rc) {
+        release(c, db.d, db.bytes);
+        return rc;
+    }
+    cudaError_t err = cudaMemcpyAsync(dev.p, planes, db.L.words * 8, cudaMemcpyHostToDevice, c->st);
+    if (err == cudaSuccess) err = launch_db_import(dev.as<uint32_t>(), db.L, db.d, c->st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(c->st);
+    if (err != cudaSuccess) {
+        release(c, db.d, db.bytes);
+        return fail(SP_ERR_CUDA, std::string("database import: ") + cudaGetErrorString(err));
+    }
+    c->dbs[db_id] = db;
+    return SP_OK;
+}
+
+int sp_db_unload(sp_ctx *c, int32_t db_id) {
+    if (!c) return fail(SP_ERR_INVALID, "NULL context");
+    std::lock_guard<std::mutex> lk(c->mu);
+    auto it = c->dbs.find(db_id);
+    if (it == c->dbs.end()) return fail(SP_ERR_NOT_FOUND, "unknown database id");
+    CU(cudaStreamSynchronize(c->st));
+    release(c, it->second.d, it->second.bytes);
+    c->dbs.erase(it);
+    return SP_OK;
+}
+
+// ----------------------------------------------------------------- clients
+static int evict_lru(sp_ctx *c, uint64_t need) {
+    while (c->budget && c->used + need > c->budget && !c->clients.empty()) {
+        auto victim = c->clients.begin();
+        for (auto it = c->clients.begin(); it != c->clients.end(); ++it)
+            if (it->second.stamp < victim->second.stamp) victim = it;
+        release(c, victim->second.keys, victim->second.bytes);
+        c->clients.erase(victim);
+    }
+    return SP_OK;
+}
+
+int sp_client_set_keys(sp_ctx *c, int32_t client_id, const uint64_t *exp_left, int32_t n_left,
+                       const uint64_t *exp_right, int32_t n_right, const uint64_t *conv, const uint64_t *pack) {
+    if (!c || !exp_left || !exp_right || !conv || !pack) return fail(SP_ERR_INVALID, "NULL argument");
+    if (n_left < 1 || n_left > LOGD || n_right < 1 || n_right > LOGD)
+        return fail(SP_ERR_INVALID, "expansion key counts must be in [1, 11]");
+    std::lock_guard<std::mutex> lk(c->mu);
+    const StageParams &s = c->sp;
+    const uint64_t P = 2ull * D;   // words per NTT poly
+    const uint64_t wl = (uint64_t)n_left * 2 * s.t_left * P, wr = (uint64_t)n_right * 2 * s.t_right * P;
+    const uint64_t wc = 2ull * 2 * s.t_conv * P, wp = (uint64_t)s.n * (s.n + 1) * s.t_conv * P;
+    const uint64_t words = wl + wr + wc + wp;
+    CU(cudaStreamSynchronize(c->st));
+    auto old = c->clients.find(client_id);
+    if (old != c->clients.end()) {
+        release(c, old->second.keys, old->second.bytes);
+        c->clients.erase(old);
+    }
+    evict_lru(c, words * 4 + words * 8);
+    Client cl;
+    cl.n_left = n_left;
+    cl.n_right = n_right;
+    cl.bytes = words * 4;
+    TRY(alloc(c, (void **)&cl.keys, cl.bytes));
+    Tmp up(c);
+    int rc = up.get(words * 8);
+    if (rc) {
+        release(c, cl.keys, cl.bytes);
+        return rc;
+    }
+    uint64_t *u = up.as<uint64_t>();
+    cudaError_t e = cudaSuccess;
+    const uint64_t *src[4] = {exp_left, exp_right, conv, pack};
+    const uint64_t cnt[4] = {wl, wr, wc, wp};
+    uint64_t off = 0;
+    for (int i = 0; i < 4 && e == cudaSuccess; i++) {
+        e = cudaMemcpyAsync(u + off, src[i], cnt[i] * 8, cudaMemcpyHostToDevice, c->st);
+        off += cnt[i];
+    }
+    if (e == cudaSuccess) e = launch_narrow(u, cl.keys, words / D, true, c->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+    if (e != cudaSuccess) {
+        release(c, cl.keys, cl.bytes);
+        return fail(SP_ERR_CUDA, std::string("key upload: ") + cudaGetErrorString(e));
+    }
+    cl.left = cl.keys;
+    cl.right = cl.keys + wl;
+    cl.conv = cl.keys + wl + wr;
+    cl.pack = cl.keys + wl + wr + wc;
+    cl.stamp = ++c->clock;
+    c->clients[client_id] = cl;
+    return SP_OK;
+}
+
+int sp_client_evict(sp_ctx *c, int32_t client_id) {
+    if (!c) return fail(SP_ERR_INVALID, "NULL context");
+    std::lock_guard<std::mutex> lk(c->mu);
+    auto it = c->clients.find(client_id);
+    if (it == c->clients.end()) return fail(SP_ERR_NOT_FOUND, "unknown client id");
+    CU(cudaStreamSynchronize(c->st));
+    release(c, it->second.keys, it->second.bytes);
+    c->clients.erase(it);
+    return SP_OK;
+}
+
+// --------------------------------------------------------------- answering
+// Validate requests and fill slots [0, n) with descriptors (queries copied
+// in from host memory).  Requests are ordered by database so that each
+// database's multiply is one launch.
+static int prepare(sp_ctx *c, int n, sp_request *reqs, std::vector<int> &order, std::vector<int> &db_of_slot) {
+    if (n < 1 || n > c->p.max_batch) return fail(SP_ERR_INVALID, "batch size out of range");
+    Shape need{};
+    for (int i = 0; i < n; i++) {
+        sp_request &r = reqs[i];
+        if (!r.query || !r.response) return fail(SP_ERR_INVALID, "NULL query or response");
+        if (r.response_len < response_bytes(c->sp)) return fail(SP_ERR_INVALID, "response buffer too small");
+        auto ci = c->clients.find(r.client_id);
+        if (ci == c->clients.end()) return fail(SP_ERR_NOT_FOUND, "unknown client id " + std::to_string(r.client_id));
+        auto di = c->dbs.find(r.db_id);
+        if (di == c->dbs.end()) return fail(SP_ERR_NOT_FOUND, "unknown database id " + std::to_string(r.db_id));
+        int nl, nr;
+        TRY(check_client_for(c, ci->second, di->second, &nl, &nr));
+        Shape s = shape_of(c, di->second.L.nu1, di->second.L.nu2);
+        need.nu1 = std::max(need.nu1, s.nu1);
+        need.nu2 = std::max(need.nu2, s.nu2);
+        need.g = std::max(need.g, s.g);
+    }
+    TRY(ensure_slots(c, need, n));
+    order.resize(n);
+    for (int i = 0; i < n; i++) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return reqs[a].db_id < reqs[b].db_id; });
+    db_of_slot.resize(n);
+    for (int k = 0; k < n; k++) {
+        sp_request &r = reqs[order[k]];
+        Slot &sl = c->slots[k];
+        Client &cl = c->clients[r.client_id];
+        cl.stamp = ++c->clock;
+        fill_desc(c, sl.q, cl, c->dbs[r.db_id]);
+        sl.client = r.client_id;
+        sl.db = r.db_id;
+        c->h_qd[k] = sl.q;
+        db_of_slot[k] = r.db_id;
+        CU(cudaMemcpyAsync(sl.query64, r.query, 4ull * D * 8, cudaMemcpyHostToDevice, c->st));
+        CU(launch_narrow(sl.query64, sl.query32, 4, false, c->st));   // 2 rows x 2 primes
+    }
+    CU(cudaMemcpyAsync(c->d_qd, c->h_qd, sizeof(QDesc) * n, cudaMemcpyHostToDevice, c->st));
+    return SP_OK;
+}
+
+int sp_answer_batch(sp_ctx *c, int32_t count, sp_request *reqs) {
+    if (!c || !reqs) return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    std::vector<int> order, dbs;
+    int rc = prepare(c, count, reqs, order, dbs);
+    if (!rc) rc = run_pipeline(c, count, dbs);
+    if (!rc) {
+        const uint64_t rb = response_bytes(c->sp);
+        for (int k = 0; k < count && !rc; k++) {
+            cudaError_t e = cudaMemcpyAsync(reqs[order[k]].response, c->slots[k].q.resp, rb,
+                                            cudaMemcpyDeviceToHost, c->st);
+            if (e != cudaSuccess) rc = fail(SP_ERR_CUDA, std::string("response copy: ") + cudaGetErrorString(e));
+        }
+    }
+    if (!rc) rc = check_device_err(c);
+    if (!rc) rc = collect_stats(c);
+    c->staged = 0;
+    for (int i = 0; i < count; i++) reqs[i].status = rc;
+    return rc;
+}
+
+int sp_answer(sp_ctx *c, int32_t client_id, int32_t db_id, const uint64_t *query, uint8_t *response,
+              uint64_t response_len) {
+    sp_request r{client_id, db_id, query, response, response_len, 0};
+    return sp_answer_batch(c, 1, &r);
+}
+
+int sp_stage_query(sp_ctx *c, int32_t slot, int32_t client_id, int32_t db_id, const uint64_t *query) {
+    if (!c || !query) return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (slot < 0 || slot >= c->p.max_batch) return fail(SP_ERR_INVALID, "slot out of range");
+    auto ci = c->clients.find(client_id);
+    auto di = c->dbs.find(db_id);
+    if (ci == c->clients.end() || di == c->dbs.end()) return fail(SP_ERR_NOT_FOUND, "unknown client or database");
+    int nl, nr;
+    TRY(check_client_for(c, ci->second, di->second, &nl, &nr));
+    TRY(ensure_slots(c, shape_of(c, di->second.L.nu1, di->second.L.nu2), slot + 1));
+    Slot &sl = c->slots[slot];
+    fill_desc(c, sl.q, ci->second, di->second);
+    sl.client = client_id;
+    sl.db = db_id;
+    c->h_qd[slot] = sl.q;
+    CU(cudaMemcpyAsync(sl.query64, query, 4ull * D * 8, cudaMemcpyHostToDevice, c->st));
+    CU(launch_narrow(sl.query64, sl.query32, 4, false, c->st));   // 2 rows x 2 primes
+    CU(cudaMemcpyAsync(c->d_qd + slot, &c->h_qd[slot], sizeof(QDesc), cudaMemcpyHostToDevice, c->st));
+    CU(cudaStreamSynchronize(c->st));
+    c->staged = std::max(c->staged, slot + 1);
+    return SP_OK;
+}
+
+int sp_run_staged(sp_ctx *c, int32_t count) {
+    if (!c) return fail(SP_ERR_INVALID, "NULL context");
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (count < 1 || count > c->staged) return fail(SP_ERR_INVALID, "count exceeds staged queries");
+    std::vector<int> dbs(count);
+    for (int k = 0; k < count; k++) {
+        dbs[k] = c->slots[k].db;
+        if (!c->dbs.count(dbs[k]) || !c->clients.count(c->slots[k].client))
+            return fail(SP_ERR_NOT_FOUND, "staged query refers to an unloaded database or client");
+    }
+    for (int k = 1; k < count; k++)
+        if (dbs[k] < dbs[k - 1]) return fail(SP_ERR_INVALID, "stage slots in database order");
+    TRY(run_pipeline(c, count, dbs));
+    TRY(check_device_err(c));
+    return collect_stats(c);
+}
+
+int sp_time_staged(sp_ctx *c, int32_t count, int32_t iters, double *ms_per_run) {
+    if (!c || !ms_per_run) return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (count < 1 || count > c->staged || iters < 1) return fail(SP_ERR_INVALID, "count/iters out of range");
+    std::vector<int> dbs(count);
+    for (int k = 0; k < count; k++) dbs[k] = c->slots[k].db;
+    cudaEvent_t a, b;
+    CU(cudaEventCreate(&a));
+    CU(cudaEventCreate(&b));
+    int rc = SP_OK;
+    float tot = 0;
+    if (cudaEventRecord(a, c->st) != cudaSuccess) rc = fail(SP_ERR_CUDA, "event record failed");
+    for (int i = 0; i < iters && !rc; i++) rc = run_pipeline(c, count, dbs);
+    if (!rc && cudaEventRecord(b, c->st) != cudaSuccess) rc = fail(SP_ERR_CUDA, "event record failed");
+    if (!rc) rc = check_device_err(c);
+    if (!rc && cudaEventElapsedTime(&tot, a, b) != cudaSuccess) rc = fail(SP_ERR_CUDA, "event time failed");
+    if (!rc) rc = collect_stats(c);   // stage split of the last run only
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    if (!rc) *ms_per_run = tot / iters;
+    return rc;
+}
+
+int sp_fetch_response(sp_ctx *c, int32_t slot, uint8_t *response, uint64_t response_len) {
+    if (!c || !response) return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (slot < 0 || slot >= (int)c->slots.size()) return fail(SP_ERR_INVALID, "slot out of range");
+    const uint64_t rb = response_bytes(c->sp);
+    if (response_len < rb) return fail(SP_ERR_INVALID, "response buffer too small");
+    CU(cudaMemcpyAsync(response, c->slots[slot].q.resp, rb, cudaMemcpyDeviceToHost, c->st));
+    CU(cudaStreamSynchronize(c->st));
+    return SP_OK;
+}
+
+int sp_stats(sp_ctx *c, sp_stats_out *out) {
+    if (!c || !out) return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    *out = c->stats;
+    return SP_OK;
+}
+
+int sp_stats_reset(sp_ctx *c) {
+    if (!c) return fail(SP_ERR_INVALID, "NULL context");
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->stats = sp_stats_out{};
+    return SP_OK;
+}
+
+int sp_time_db_mul(sp_ctx *c, int32_t db_id, int32_t nq, int32_t iters, double *ms_per_launch) {
+    if (!c || !ms_per_launch) return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    auto di = c->dbs.find(db_id);
+    if (di == c->dbs.end()) return fail(SP_ERR_NOT_FOUND, "unknown database id");
+    if (nq < 1 || nq > c->staged || iters < 1) return fail(SP_ERR_INVALID, "nq/iters out of range");
+    for (int k = 0; k < nq; k++)
+        if (c->slots[k].db != db_id) return fail(SP_ERR_INVALID, "staged slots must query this database");
+    CU(cudaEventRecord(c->ev[0], c->st));
+    for (int i = 0; i < iters; i++) CU(launch_db_mul(di->second.d, di->second.L, c->d_qd, nq, c->d_err, c->st));
+    CU(cudaEventRecord(c->ev[1], c->st));
+    TRY(check_device_err(c));
+    float ms = 0;
+    CU(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+    *ms_per_launch = ms / iters;
+    return SP_OK;
+}
+
+// ---------------------------------------------------------- stage entries
+int sp_ntt_fwd(sp_ctx *c, const uint64_t *raw, uint64_t *crt, uint64_t count) {
+    if (!c || !raw || !crt || !count) return fail(SP_ERR_INVALID, "NULL argument or zero count");
+    std::lock_guard<std::mutex> lk(c->mu);
+    Tmp a(c), b(c);
+    TRY(a.get(count * D * 8));
+    TRY(b.get(count * 2 * D * 8));
+    CU(cudaMemcpyAsync(a.p, raw, count * D * 8, cudaMemcpyHostToDevice, c->st));
+    CU(launch_to_ntt(a.as<uint64_t>(), b.as<uint32_t>(), (int)count, c->d_tw, c->st));
+    Tmp w(c);
+    TRY(w.get(count * 2 * D * 8));
+    CU(launch_widen(b.as<uint32_t>(), w.as<uint64_t>(), count * 2, false, c->st));
+    CU(cudaMemcpyAsync(crt, w.p, count * 2 * D * 8, cudaMemcpyDeviceToHost, c->st));
+    CU(cudaStreamSynchronize(c->st));
+    return SP_OK;
+}
+
+int sp_ntt_inv(sp_ctx *c, const uint64_t *crt, uint64_t *raw, uint64_t count) {
+    if (!c || !raw || !crt || !count) return fail(SP_ERR_INVALID, "NULL argument or zero count");
+    std::lock_guard<std::mutex> lk(c->mu);
+    Tmp a(c), n(c), o(c);
+    TRY(a.get(count * 2 * D * 8));
+    TRY(n.get(count * 2 * D * 4));
+    TRY(o.get(count * D * 8));
+    CU(cudaMemcpyAsync(a.p, crt, count * 2 * D * 8, cudaMemcpyHostToDevice, c->st));
+    CU(launch_narrow(a.as<uint64_t>(), n.as<uint32_t>(), count * 2, false, c->st));
+    CU(launch_from_ntt(n.as<uint32_t>(), o.as<uint64_t>(), (int)count, c->d_tw, c->st));
+    CU(cudaMemcpyAsync(raw, o.p, count * D * 8, cudaMemcpyDeviceToHost, c->st));
+    CU(cudaStreamSynchronize(c->st));
+    return SP_OK;
+}
+
+int sp_automorph(sp_ctx *c, const uint64_t *raw, uint64_t *out, uint64_t count, uint32_t t) {
+    if (!c || !raw || !out || !count) return fail(SP_ERR_INVALID, "NULL argument or zero count");
+    if (!(t & 1)) return fail(SP_ERR_INVALID, "automorphism exponent must be odd");
+    std::lock_guard<std::mutex> lk(c->mu);
+    Tmp a(c), b(c);
+    TRY(a.get(count * D * 8));
+    TRY(b.get(count * D * 8));
+    CU(cudaMemcpyAsync(a.p, raw, count * D * 8, cudaMemcpyHostToDevice, c->st));
+    CU(launch_automorph(a.as<uint64_t>(), b.as<uint64_t>(), (int)count, t, c->st));
+    CU(cudaMemcpyAsync(out, b.p, count * D * 8, cudaMemcpyDeviceToHost, c->st));
+    CU(cudaStreamSynchronize(c->st));
+    return SP_OK;
+}
+
+int sp_expand(sp_ctx *c, int32_t client_id, const uint64_t *query, int32_t nu1, int32_t nu2, int32_t rounds,
+              uint64_t *out) {
+    if (!c || !query || !out) return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    auto ci = c->clients.find(client_id);
+    if (ci == c->clients.end()) return fail(SP_ERR_NOT_FOUND, "unknown client id");
+    if (nu1 < 1 || nu2 < 1 || nu1 > 14 || nu2 > 14) return fail(SP_ERR_INVALID, "nu1/nu2 out of range");
+    const Shape s = shape_of(c, nu1, nu2);
+    if (s.g > LOGD) return fail(SP_ERR_UNSUPPORTED, "expansion needs more than 11 rounds");
+    const int stop = ceil_log2((uint64_t)c->sp.t_gsw * nu2);
+    if (rounds <= 0) rounds = s.g;
+    if (rounds > s.g) return fail(SP_ERR_INVALID, "rounds exceeds g for this shape");
+    const Client &cl = ci->second;
+    if (cl.n_left < rounds || cl.n_right < std::min(rounds, stop + 1))
+        return fail(SP_ERR_INVALID, "client keys do not cover the requested rounds");
+    const uint64_t ct = 4ull * D;
+    const uint64_t nout = 1ull << rounds;
+    const int max_bits = c->sp.t_gsw * nu2;
+    Tmp q64(c), q32(c), v0(c), v1(c), gin(c), qd(c), w(c);
+    TRY(q64.get(ct * 8));
+    TRY(q32.get(ct * 4));
+    TRY(v0.get(ct * 4 * nout));
+    TRY(v1.get(ct * 4 * nout));
+    TRY(gin.get(ct * 4 * std::max(1, max_bits)));
+    TRY(qd.get(sizeof(QDesc)));
+    TRY(w.get(ct * 8 * nout));
+    QDesc d{};
+    d.left = cl.left;
+    d.right = cl.right;
+    d.query = q32.as<uint32_t>();
+    d.v[0] = v0.as<uint32_t>();
+    d.v[1] = v1.as<uint32_t>();
+    d.gsw_in = gin.as<uint32_t>();
+    d.sel = nullptr;
+    d.nu1 = nu1;
+    d.nu2 = nu2;
+    d.g = rounds + 1;            // every executed round writes its outputs
+    d.stop = stop;
+    d.capture = (stop > 0 && stop < rounds) ? stop : rounds;   // captured only when pruning starts
+    d.active = 1;
+    CU(cudaMemsetAsync(v0.p, 0, ct * 4 * nout, c->st));
+    CU(cudaMemsetAsync(v1.p, 0, ct * 4 * nout, c->st));
+    CU(cudaMemcpyAsync(q64.p, query, ct * 8, cudaMemcpyHostToDevice, c->st));
+    CU(launch_narrow(q64.as<uint64_t>(), q32.as<uint32_t>(), 4, false, c->st));
+    CU(cudaMemcpyAsync(qd.p, &d, sizeof(QDesc), cudaMemcpyHostToDevice, c->st));
+    for (int r = 0; r < rounds; r++)
+        CU(launch_expand_round(qd.as<QDesc>(), 1, r, 2 << r, c->sp, c->d_tw, c->d_neg1, c->st));
+    uint32_t *fin = (rounds & 1) ? d.v[1] : d.v[0];
+    // Entries pruned in the last round(s) are zero; odd entries frozen at
+    // stop_round come from the capture buffer.
+    if (d.capture < rounds) {
+        // clear odd entries of the final buffer, then copy the captured ones in
+        for (uint64_t i = 1; i < nout; i += 2)
+            CU(cudaMemsetAsync(fin + i * ct, 0, ct * 4, c->st));
+        for (int k = 0; k < max_bits && (uint64_t)(2 * k + 1) < nout; k++)
+            CU(cudaMemcpyAsync(fin + (2ull * k + 1) * ct, gin.as<uint32_t>() + (uint64_t)k * ct, ct * 4,
+                               cudaMemcpyDeviceToDevice, c->st));
+    }
+    CU(launch_widen(fin, w.as<uint64_t>(), nout * 4, false, c->st));
+    CU(cudaMemcpyAsync(out, w.p, ct * 8 * nout, cudaMemcpyDeviceToHost, c->st));
+    CU(cudaStreamSynchronize(c->st));
+    return SP_OK;
+}
+
+int sp_regev_to_gsw(sp_ctx *c, int32_t client_id, const uint64_t *regev, int32_t nu2, uint64_t *gsw) {
+    if (!c || !regev || !gsw) return fail(SP_ERR_INVALID, "NULL argument");
+    if (nu2 < 1 || nu2 > 14) return fail(SP_ERR_INVALID, "nu2 out of range");
+    std::lock_guard<std::mutex> lk(c->mu);
+    auto ci = c->clients.find(client_id);
+    if (ci == c->clients.end()) return fail(SP_ERR_NOT_FOUND, "unknown client id");
+    const uint64_t ct = 4ull * D;
+    const int nin = nu2 * c->sp.t_gsw;
+    const uint64_t gwords = (uint64_t)nu2 * 2 * 2 * c->sp.t_gsw * 2 * D;
+    Tmp a(c), b(c), g(c), w(c), qd(c);
+    TRY(a.get(ct * 8 * nin));
+    TRY(b.get(ct * 4 * nin));
+    TRY(g.get(gwords * 4));
+    TRY(w.get(gwords * 8));
+    TRY(qd.get(sizeof(QDesc)));
+    QDesc d{};
+    d.conv = ci->second.conv;
+    d.gsw_in = b.as<uint32_t>();
+    d.gsw = g.as<uint32_t>();
+    d.nu2 = nu2;
+    d.active = 1;
+    CU(cudaMemcpyAsync(a.p, regev, ct * 8 * nin, cudaMemcpyHostToDevice, c->st));
+    CU(launch_narrow(a.as<uint64_t>(), b.as<uint32_t>(), (uint64_t)nin * 4, false, c->st));
+    CU(cudaMemcpyAsync(qd.p, &d, sizeof(QDesc), cudaMemcpyHostToDevice, c->st));
+    CU(launch_regev_to_gsw(qd.as<QDesc>(), 1, nin, c->sp, c->d_tw, c->st));
+    CU(launch_widen(g.as<uint32_t>(), w.as<uint64_t>(), gwords / D, true, c->st));
+    CU(cudaMemcpyAsync(gsw, w.p, gwords * 8, cudaMemcpyDeviceToHost, c->st));
+    CU(cudaStreamSynchronize(c->st));
+    return SP_OK;
+}
+
+int sp_gsw_neg(sp_ctx *c, const uint64_t *gsw, int32_t count, uint64_t *neg) {
+    if (!c || !gsw || !neg || count < 1) return fail(SP_ERR_INVALID, "NULL argument or bad count");
+    std::lock_guard<std::mutex> lk(c->mu);
+    const uint64_t words = (uint64_t)count * 2 * 2 * c->sp.t_gsw * 2 * D;
+    Tmp a(c), b(c), o(c);
+    TRY(a.get(words * 8));
+    TRY(b.get(words * 4));
+    TRY(o.get(words * 4));
+    CU(cudaMemcpyAsync(a.p, gsw, words * 8, cudaMemcpyHostToDevice, c->st));
+    CU(launch_narrow(a.as<uint64_t>(), b.as<uint32_t>(), words / D, false, c->st));
+    CU(launch_gsw_neg(b.as<uint32_t>(), o.as<uint32_t>(), count, c->sp.t_gsw, c->st));
+    CU(launch_widen(o.as<uint32_t>(), a.as<uint64_t>(), words / D, false, c->st));
+    CU(cudaMemcpyAsync(neg, a.p, words * 8, cudaMemcpyDeviceToHost, c->st));
+    CU(cudaStreamSynchronize(c->st));
+    return SP_OK;
+}
+
+int sp_db_mul(sp_ctx *c, int32_t db_id, const uint64_t *sel, uint64_t *acc) {
+    if (!c || !sel || !acc) return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    auto di = c->dbs.find(db_id);
+    if (di == c->dbs.end()) return fail(SP_ERR_NOT_FOUND, "unknown database id");
+    const DbLayout &L = di->second.L;
+    const uint64_t sel_words = (uint64_t)L.rows * 4 * D;
+    const uint64_t acc_words = (uint64_t)L.T * L.cols * 4 * D;
+    Tmp a(c), s(c), o(c), w(c), qd(c);
+    TRY(a.get(sel_words * 8));
+    TRY(s.get(sel_words * 4));
+    TRY(o.get(acc_words * 4));
+    TRY(w.get(acc_words * 8));
+    TRY(qd.get(sizeof(QDesc)));
+    QDesc d{};
+    d.sel = s.as<uint32_t>();
+    d.acc = o.as<uint32_t>();
+    d.nu1 = L.nu1;
+    d.nu2 = L.nu2;
+    d.active = 1;
+    CU(cudaMemcpyAsync(a.p, sel, sel_words * 8, cudaMemcpyHostToDevice, c->st));
+    CU(launch_sel_import(a.as<uint64_t>(), s.as<uint32_t>(), L.rows, c->st));
+    CU(cudaMemcpyAsync(qd.p, &d, sizeof(QDesc), cudaMemcpyHostToDevice, c->st));
+    CU(launch_db_mul(di->second.d, L, qd.as<QDesc>(), 1, c->d_err, c->st));
+    CU(launch_widen(o.as<uint32_t>(), w.as<uint64_t>(), acc_words / D, false, c->st));
+    CU(cudaMemcpyAsync(acc, w.p, acc_words * 8, cudaMemcpyDeviceToHost, c->st));
+    TRY(check_device_err(c));
+    return SP_OK;
+}
+
+int sp_fold(sp_ctx *c, const uint64_t *cts, const uint64_t *gsw, int32_t T, int32_t nu2, uint64_t *out) {
+    if (!c || !cts || !gsw || !out) return fail(SP_ERR_INVALID, "NULL argument");
+    if (T < 1 || T > c->sp.T || nu2 < 1 || nu2 > 14) return fail(SP_ERR_INVALID, "T or nu2 out of range");
+    std::lock_guard<std::mutex> lk(c->mu);
+    const uint64_t raw_words = ((uint64_t)T * 2 * D) << nu2;
+    const uint64_t gwords = (uint64_t)nu2 * 2 * 2 * c->sp.t_gsw * 2 * D;
+    Tmp r(c), g64(c), g(c), qd(c);
+    TRY(r.get(raw_words * 8));
+    TRY(g64.get(gwords * 8));
+    TRY(g.get(gwords * 4));
+    TRY(qd.get(sizeof(QDesc)));
+    QDesc d{};
+    d.raw = r.as<uint64_t>();
+    d.gsw = g.as<uint32_t>();
+    d.nu2 = nu2;
+    d.active = 1;
+    StageParams sp = c->sp;
+    sp.T = T;
+    CU(cudaMemcpyAsync(r.p, cts, raw_words * 8, cudaMemcpyHostToDevice, c->st));
+    CU(cudaMemcpyAsync(g64.p, gsw, gwords * 8, cudaMemcpyHostToDevice, c->st));
+    CU(launch_narrow(g64.as<uint64_t>(), g.as<uint32_t>(), gwords / D, true, c->st));
+    CU(cudaMemcpyAsync(qd.p, &d, sizeof(QDesc), cudaMemcpyHostToDevice, c->st));
+    for (int lvl = 0; lvl < nu2; lvl++)
+        CU(launch_fold_level(qd.as<QDesc>(), 1, lvl, T << (nu2 - 1 - lvl), sp, c->d_tw, c->st));
+    for (int t = 0; t < T; t++)
+        CU(cudaMemcpyAsync(out + (uint64_t)t * 2 * D, r.as<uint64_t>() + ((uint64_t)t << nu2) * 2 * D, 2ull * D * 8,
+                           cudaMemcpyDeviceToHost, c->st));
+    CU(cudaStreamSynchronize(c->st));
+    return SP_OK;
+}
+
+int sp_pack(sp_ctx *c, int32_t client_id, const uint64_t *cts, uint8_t *response, uint64_t response_len) {
+    if (!c || !cts || !response) return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    auto ci = c->clients.find(client_id);
+    if (ci == c->clients.end()) return fail(SP_ERR_NOT_FOUND, "unknown client id");
+    const uint64_t rb = response_bytes(c->sp);
+    if (response_len < rb) return fail(SP_ERR_INVALID, "response buffer too small");
+    const int T = c->sp.T, n = c->sp.n;
+    Tmp r(c), ms(c), resp(c), qd(c);
+    TRY(r.get((uint64_t)T * 2 * D * 8));
+    TRY(ms.get((uint64_t)(n + 1) * n * D * 4));
+    TRY(resp.get(rb));
+    TRY(qd.get(sizeof(QDesc)));
+    QDesc d{};
+    d.pack = ci->second.pack;
+    d.raw = r.as<uint64_t>();
+    d.ms = ms.as<uint32_t>();
+    d.resp = resp.as<uint8_t>();
+    d.nu2 = 0;   // one ciphertext per instance
+    d.active = 1;
+    CU(cudaMemcpyAsync(r.p, cts, (uint64_t)T * 2 * D * 8, cudaMemcpyHostToDevice, c->st));
+    CU(cudaMemcpyAsync(qd.p, &d, sizeof(QDesc), cudaMemcpyHostToDevice, c->st));
+    CU(launch_pack(qd.as<QDesc>(), 1, c->sp, c->d_tw, c->st));
+    CU(launch_bitpack(qd.as<QDesc>(), 1, c->sp, rb, c->st));
+    CU(cudaMemcpyAsync(response, resp.p, rb, cudaMemcpyDeviceToHost, c->st));
+    CU(cudaStreamSynchronize(c->st));
+    return SP_OK;
+}
+
+}  // extern "C"

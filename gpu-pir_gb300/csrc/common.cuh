@@ -1,0 +1,316 @@
+// Device-side building blocks of the Spiral answer path on GB300 (sm_103a).
+//
+// Ring Z_q[x]/(x^2048 + 1), q = q1*q2 with q1 = 268369921, q2 = 249561089
+// (gpu-pir/params.cuh:25-31).  NTT form is the reference's "spiral order":
+// the in-place Cooley-Tukey negacyclic transform with bit-reversed powers of
+// psi (gpu-pir/ntt_28bit.cuh:31-131, gpu-pir/host.cu:64-71).
+//
+// One residue plane (2048 values mod one prime) is transformed by a group of
+// 128 threads holding 16 values each, in three register phases separated by
+// two shared-memory transposes:
+//   layout A: thread t holds e = t + 128*j        stages h = 1024 .. 128
+//   layout B: thread t holds e = 128*(t>>3) + (t&7) + 8*j   h = 64 .. 8
+//   layout C: thread t holds e = 16*t + j         stages h = 4, 2, 1
+// Raw-domain work (digits, inverse CRT) uses layout A (coalesced), NTT-domain
+// work (key products) uses layout C (16 consecutive slots per thread).
+// Butterflies are Harvey's lazy Montgomery butterflies (values < 4p forward,
+// < 2p inverse); the transposes use an XOR swizzle that is bank-conflict free
+// for all three layouts.
+#pragma once
+#include <stdint.h>
+#include <cuda_runtime.h>
+
+namespace sp {
+
+constexpr int D = 2048;
+constexpr int LOGD = 11;
+constexpr uint32_t QP0 = 268369921u;
+constexpr uint32_t QP1 = 249561089u;
+constexpr uint64_t QQ = (uint64_t)QP0 * (uint64_t)QP1;
+constexpr int MOD_BITS = 56;
+constexpr int GROUP = 128;          // threads per NTT group
+constexpr int VPT = D / GROUP;      // values per thread (16)
+
+// ---------------------------------------------------------------- host math
+constexpr uint32_t inv32(uint32_t p) {  // p^-1 mod 2^32 (Newton)
+    uint32_t x = p;
+    for (int i = 0; i < 5; i++) x *= 2u - p * x;
+    return x;
+}
+constexpr uint64_t powmod_c(uint64_t b, uint64_t e, uint64_t m) {
+    uint64_t r = 1;
+    b %= m;
+    while (e) {
+        if (e & 1) r = r * b % m;
+        b = b * b % m;
+        e >>= 1;
+    }
+    return r;
+}
+
+struct Prime {
+    uint32_t p;
+    uint32_t pinv;      // p^-1 mod 2^32
+    uint32_t r2;        // 2^64 mod p (to Montgomery form)
+    uint32_t ninv_m;    // 2048^-1 * 2^32 mod p
+    uint32_t crt_m;     // (other prime)^-1 * 2048^-1 * 2^32 mod p
+    uint32_t two32;     // 2^32 mod p
+};
+
+constexpr Prime make_prime(uint32_t p, uint32_t other) {
+    Prime c{};
+    c.p = p;
+    c.pinv = inv32(p);
+    c.two32 = (uint32_t)((1ull << 32) % p);
+    c.r2 = (uint32_t)((uint64_t)c.two32 * c.two32 % p);
+    uint64_t ninv = powmod_c(D, p - 2, p);
+    c.ninv_m = (uint32_t)(ninv * c.two32 % p);
+    uint64_t oinv = powmod_c(other % p, p - 2, p);
+    c.crt_m = (uint32_t)(oinv * ninv % p * c.two32 % p);
+    return c;
+}
+
+constexpr Prime PRIME0_H = make_prime(QP0, QP1);
+constexpr Prime PRIME1_H = make_prime(QP1, QP0);
+// scalar copies (usable in device code)
+constexpr uint32_t P0_PINV = PRIME0_H.pinv, P1_PINV = PRIME1_H.pinv;
+constexpr uint32_t P0_R2 = PRIME0_H.r2, P1_R2 = PRIME1_H.r2;
+constexpr uint32_t P0_NINV = PRIME0_H.ninv_m, P1_NINV = PRIME1_H.ninv_m;
+constexpr uint32_t P0_CRT = PRIME0_H.crt_m, P1_CRT = PRIME1_H.crt_m;
+constexpr uint32_t P0_TWO32 = PRIME0_H.two32, P1_TWO32 = PRIME1_H.two32;
+
+__host__ __device__ __forceinline__ Prime prime_of(int k) {
+    Prime c;
+    c.p = k ? QP1 : QP0;
+    c.pinv = k ? P1_PINV : P0_PINV;
+    c.r2 = k ? P1_R2 : P0_R2;
+    c.ninv_m = k ? P1_NINV : P0_NINV;
+    c.crt_m = k ? P1_CRT : P0_CRT;
+    c.two32 = k ? P1_TWO32 : P0_TWO32;
+    return c;
+}
+
+// ------------------------------------------------------------ device math
+__device__ __forceinline__ uint32_t mont_mul(uint32_t a, uint32_t b, uint32_t p, uint32_t pinv) {
+    // a < 2^32, b < p  ->  a*b*2^-32 mod p in (0, 2p)
+    uint64_t u = (uint64_t)a * b;
+    uint32_t m = (uint32_t)u * pinv;
+    return (uint32_t)(u >> 32) - __umulhi(m, p) + p;
+}
+
+__device__ __forceinline__ uint32_t reduce2(uint32_t x, uint32_t twop) {  // [0,2*twop) -> [0,twop)
+    return min(x, x - twop);
+}
+
+__device__ __forceinline__ uint32_t canon4(uint32_t x, uint32_t p) {  // [0,4p) -> [0,p)
+    x = min(x, x - 2 * p);
+    return min(x, x - p);
+}
+
+// x (< 2^56 or any u64 < p*2^32) mod p, canonical
+__device__ __forceinline__ uint32_t mod_u64(uint64_t x, const Prime &c) {
+    uint32_t lo = (uint32_t)x, hi = (uint32_t)(x >> 32);
+    // x*2^-32 mod p via Montgomery reduction of (hi:lo)
+    uint32_t m = lo * c.pinv;
+    uint32_t r = hi - __umulhi(m, c.p) + c.p;       // (0, 2p) when hi < p
+    r = mont_mul(r, c.r2, c.p, c.pinv);             // * 2^64 * 2^-32 -> x
+    return min(r, r - c.p);
+}
+
+// Inverse CRT of unscaled INTT outputs a0 (mod q1) and a1 (mod q2), both in
+// [0, 2p): returns x in [0, q) with x = 2048^-1 * CRT(a0, a1).
+__device__ __forceinline__ uint64_t icrt(uint32_t a0, uint32_t a1) {
+    uint32_t x0 = mont_mul(a0, P0_CRT, QP0, P0_PINV);
+    x0 = min(x0, x0 - QP0);
+    uint32_t x1 = mont_mul(a1, P1_CRT, QP1, P1_PINV);
+    x1 = min(x1, x1 - QP1);
+    uint64_t s = (uint64_t)x0 * QP1 + (uint64_t)x1 * QP0;
+    return s >= QQ ? s - QQ : s;
+}
+
+// ------------------------------------------------------------- barriers
+__device__ __forceinline__ void group_sync(int bar_id) {
+    asm volatile("bar.sync %0, %1;" ::"r"(bar_id), "n"(GROUP) : "memory");
+}
+
+// -------------------------------------------------------------- swizzle
+// Bank of element e: bits (e0^e5, e1^e6, e2^e8, e3^e7, e4^e8).  Linear in
+// the bits of e, so swz(a | b) = swz(a) ^ swz(b) for disjoint bit sets.
+__host__ __device__ __forceinline__ constexpr int swz(int e) {
+    return e ^ (((e >> 5) & 1) | (((e >> 6) & 1) << 1) | (((e >> 8) & 1) << 2) |
+                (((e >> 7) & 1) << 3) | (((e >> 8) & 1) << 4));
+}
+
+// --------------------------------------------------------- twiddle tables
+// Per (prime, direction): 2048 u32 in Montgomery form.  Entry m+i holds
+// psi^(+-brev11(m+i)) (block i of the stage with m blocks) for m < 256; the
+// last three stages (m = 256, 512, 1024; c = m/128 twiddles per thread) are
+// restrided so that entry m + k*128 + t holds twiddle m + c*t + k.
+struct TwiddleSet {
+    uint32_t t[4][D];   // [fwd q1, fwd q2, inv q1, inv q2]
+};
+
+// -------------------------------------------------------- NTT butterflies
+__device__ __forceinline__ void ct_bfly(uint32_t &x, uint32_t &y, uint32_t w, uint32_t p, uint32_t pinv) {
+    uint32_t xr = min(x, x - 2 * p);
+    uint32_t t = mont_mul(y, w, p, pinv);
+    x = xr + t;
+    y = xr - t + 2 * p;
+}
+
+__device__ __forceinline__ void gs_bfly(uint32_t &x, uint32_t &y, uint32_t w, uint32_t p, uint32_t pinv) {
+    uint32_t s = x + y;
+    uint32_t d = x - y + 2 * p;
+    x = min(s, s - 2 * p);
+    y = mont_mul(d, w, p, pinv);
+}
+
+// Per-thread address bases of the three layouts (t: thread within group).
+__device__ __forceinline__ int baseA(int t) { return swz(t); }
+__device__ __forceinline__ int baseB(int t) { return swz(128 * (t >> 3) + (t & 7)); }
+__device__ __forceinline__ int baseC(int t) { return swz(16 * t); }
+
+// Forward NTT of one plane.  v: layout A in (values < 4p), layout C out
+// (values < 4p).  tw: forward table of this prime (shared or global).
+// buf: 2 x 2048 words of shared memory private to the group.
+__device__ __forceinline__ void ntt_fwd(uint32_t (&v)[VPT], const uint32_t *__restrict__ tw,
+                                        uint32_t *buf, const Prime &c, int t, int bar_id) {
+    const uint32_t p = c.p, pinv = c.pinv;
+    // phase A: h = 1024, 512, 256, 128  (pairs j, j + 8>>L)
+#pragma unroll
+    for (int L = 0; L < 4; L++) {
+        const int dj = 8 >> L;
+#pragma unroll
+        for (int j = 0; j < VPT; j++)
+            if ((j & dj) == 0) ct_bfly(v[j], v[j + dj], tw[(1 << L) + j / (2 * dj)], p, pinv);
+    }
+    // transpose A -> B
+    {
+        uint32_t *b0 = buf;
+        const int a = baseA(t);
+#pragma unroll
+        for (int j = 0; j < VPT; j++) b0[a ^ swz(128 * j)] = v[j];
+        group_sync(bar_id);
+        const int b = baseB(t);
+#pragma unroll
+        for (int j = 0; j < VPT; j++) v[j] = b0[b ^ swz(8 * j)];
+    }
+    // phase B: h = 64, 32, 16, 8
+    {
+        const int bb = t >> 3;
+#pragma unroll
+        for (int L = 4; L < 8; L++) {
+            const int dj = 8 >> (L - 4);
+#pragma unroll
+            for (int j = 0; j < VPT; j++)
+                if ((j & dj) == 0)
+                    ct_bfly(v[j], v[j + dj], tw[(1 << L) + (bb << (L - 4)) + (j >> (8 - L))], p, pinv);
+        }
+    }
+    // transpose B -> C
+    {
+        uint32_t *b1 = buf + D;
+        const int b = baseB(t);
+#pragma unroll
+        for (int j = 0; j < VPT; j++) b1[b ^ swz(8 * j)] = v[j];
+        group_sync(bar_id);
+        const int cc = baseC(t);
+#pragma unroll
+        for (int j = 0; j < VPT; j++) v[j] = b1[cc ^ j];
+    }
+    // phase C: h = 4, 2, 1 (restrided twiddles)
+#pragma unroll
+    for (int L = 8; L < 11; L++) {
+        const int dj = 4 >> (L - 8);
+#pragma unroll
+        for (int j = 0; j < VPT; j++)
+            if ((j & dj) == 0) ct_bfly(v[j], v[j + dj], tw[(1 << L) + (j / (2 * dj)) * GROUP + t], p, pinv);
+    }
+}
+
+// Inverse NTT of one plane (without the 2048^-1 scaling).  v: layout C in
+// (values < 2p), layout A out (values < 2p).
+__device__ __forceinline__ void ntt_inv(uint32_t (&v)[VPT], const uint32_t *__restrict__ tw,
+                                        uint32_t *buf, const Prime &c, int t, int bar_id) {
+    const uint32_t p = c.p, pinv = c.pinv;
+#pragma unroll
+    for (int L = 10; L >= 8; L--) {
+        const int dj = 4 >> (L - 8);
+#pragma unroll
+        for (int j = 0; j < VPT; j++)
+            if ((j & dj) == 0) gs_bfly(v[j], v[j + dj], tw[(1 << L) + (j / (2 * dj)) * GROUP + t], p, pinv);
+    }
+    {
+        uint32_t *b0 = buf;
+        const int cc = baseC(t);
+#pragma unroll
+        for (int j = 0; j < VPT; j++) b0[cc ^ j] = v[j];
+        group_sync(bar_id);
+        const int b = baseB(t);
+#pragma unroll
+        for (int j = 0; j < VPT; j++) v[j] = b0[b ^ swz(8 * j)];
+    }
+    {
+        const int bb = t >> 3;
+#pragma unroll
+        for (int L = 7; L >= 4; L--) {
+            const int dj = 8 >> (L - 4);
+#pragma unroll
+            for (int j = 0; j < VPT; j++)
+                if ((j & dj) == 0)
+                    gs_bfly(v[j], v[j + dj], tw[(1 << L) + (bb << (L - 4)) + (j >> (8 - L))], p, pinv);
+        }
+    }
+    {
+        uint32_t *b1 = buf + D;
+        const int b = baseB(t);
+#pragma unroll
+        for (int j = 0; j < VPT; j++) b1[b ^ swz(8 * j)] = v[j];
+        group_sync(bar_id);
+        const int a = baseA(t);
+#pragma unroll
+        for (int j = 0; j < VPT; j++) v[j] = b1[a ^ swz(128 * j)];
+    }
+#pragma unroll
+    for (int L = 3; L >= 0; L--) {
+        const int dj = 8 >> L;
+#pragma unroll
+        for (int j = 0; j < VPT; j++)
+            if ((j & dj) == 0) gs_bfly(v[j], v[j + dj], tw[(1 << L) + j / (2 * dj)], p, pinv);
+    }
+}
+
+// Copy the four twiddle tables into shared memory (all threads of the CTA).
+__device__ __forceinline__ void load_twiddles(uint32_t *dst, const TwiddleSet *src) {
+    const uint4 *s = reinterpret_cast<const uint4 *>(src);
+    uint4 *d = reinterpret_cast<uint4 *>(dst);
+    for (int i = threadIdx.x; i < 4 * D / 4; i += blockDim.x) d[i] = __ldg(s + i);
+}
+
+// Slot permutation of the automorphism x -> x^tau in NTT form: the slot z
+// evaluates at psi^(2*brev(z)+1); tau(f) at that point is f at
+// psi^((2*brev(z)+1)*tau), so out[z] = in[auto_slot(z, tau)].
+__device__ __forceinline__ int auto_slot(int z, uint32_t tau) {
+    uint32_t r = __brev((uint32_t)z) >> (32 - LOGD);
+    uint32_t e = ((2 * r + 1) * tau) & (2 * D - 1);
+    return (int)(__brev((e - 1) >> 1) >> (32 - LOGD));
+}
+
+__device__ __forceinline__ int bits_per(int t) { return (MOD_BITS + t - 1) / t; }
+
+// 16 consecutive u32 (layout C slice) load/store helpers.
+__device__ __forceinline__ void ld16(uint32_t (&v)[VPT], const uint32_t *p) {
+    const uint4 *q = reinterpret_cast<const uint4 *>(p);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        uint4 x = q[i];
+        v[4 * i] = x.x; v[4 * i + 1] = x.y; v[4 * i + 2] = x.z; v[4 * i + 3] = x.w;
+    }
+}
+__device__ __forceinline__ void st16(uint32_t *p, const uint32_t (&v)[VPT]) {
+    uint4 *q = reinterpret_cast<uint4 *>(p);
+#pragma unroll
+    for (int i = 0; i < 4; i++) q[i] = make_uint4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+}
+
+}  // namespace sp

@@ -1,0 +1,178 @@
+/*
+ * spiralpir.h - C ABI of the GB300 Spiral PIR answer path (libspiralpir.so).
+ *
+ * Drop-in for the server answer path of EricArcherman/GPU-PIR.  The
+ * reference has no callable answer API: its host boundary is gpu-pir/host.h
+ * (C++ linkage, std::string/std::vector arguments, errors call exit) and the
+ * answer flow lives in the test main()s (gpu-pir/fold_test.cu:30-94,
+ * gpu-pir/db_mul_test.cu:62-212, gpu-pir/expansion_test.cu:33-113).  Each
+ * entry point below names the reference code it replaces.
+ *
+ * Conventions
+ *  - Every function returns SP_OK (0) or an SP_ERR_* code and never exits
+ *    the process; sp_last_error() returns the calling thread's message.
+ *  - All buffers are host buffers owned by the caller; calls copy in and out.
+ *  - Polynomials use the layouts of the reference's golden vectors
+ *    (gpu-pir/test_data, written by spiral-rs): D = 2048 coefficients;
+ *      raw poly   uint64[D]          coefficients mod q = q1*q2
+ *      CRT poly   uint64[2][D]       NTT form mod q1 then mod q2, values < q_i
+ *      ciphertext [2 rows][...]      Regev ciphertext rows (-a, s*a+e+m)
+ *      matrix     [rows][cols][...]  row-major
+ *  - q1 = 268369921, q2 = 249561089 (gpu-pir/params.cuh:25-31).
+ *  - A context is internally locked; calls from several threads serialise.
+ */
+#ifndef SPIRALPIR_H
+#define SPIRALPIR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SP_OK 0
+#define SP_ERR_INVALID 1     /* bad argument, size or shape */
+#define SP_ERR_CUDA 2        /* CUDA runtime error */
+#define SP_ERR_NOMEM 3       /* device allocation failed or HBM budget exceeded */
+#define SP_ERR_NOT_FOUND 4   /* unknown database or client id */
+#define SP_ERR_DEVICE 5      /* a device-side check failed (bounded wait ran out) */
+#define SP_ERR_UNSUPPORTED 6 /* parameter combination not implemented */
+
+#define SP_D 2048
+
+typedef struct sp_ctx sp_ctx;
+
+/* Ring/gadget parameters shared by every database and client of a context.
+ * Replaces the compile-time constants of gpu-pir/params.cuh:49-71. */
+typedef struct sp_params {
+    int32_t n;           /* plaintext matrices are n x n (1 or 2) */
+    int32_t pt_bits;     /* plaintext modulus p = 2^pt_bits (<= 8) */
+    int32_t t_exp_left;  /* expansion gadget length, first-dimension branch */
+    int32_t t_exp_right; /* expansion gadget length, GSW-bit branch */
+    int32_t t_gsw;       /* GSW / folding gadget length */
+    int32_t t_conv;      /* Regev->GSW conversion and packing gadget length */
+    int32_t q2_bits;     /* response first row is switched to 2^q2_bits */
+    int32_t max_batch;   /* queries answered concurrently (workspace slots) */
+} sp_params;
+
+/* Per-stage device time accumulated since the last sp_stats_reset. */
+typedef struct sp_stats_out {
+    uint64_t answers;        /* queries answered */
+    uint64_t launches;       /* kernel launches issued by answers */
+    double ms_expand;        /* coefficient expansion */
+    double ms_convert;       /* Regev->GSW conversion */
+    double ms_db_mul;        /* first-dimension multiply */
+    double ms_fold;          /* DB output to raw + folding */
+    double ms_pack;          /* packing, modulus switch, serialisation */
+    double ms_total;         /* device time of whole answers */
+    uint64_t db_mul_calls;   /* first-dimension multiply launches */
+    uint64_t db_mul_bytes;   /* algorithmic bytes of those launches */
+} sp_stats_out;
+
+/* One request of a batch. */
+typedef struct sp_request {
+    int32_t client_id;
+    int32_t db_id;
+    const uint64_t *query;   /* NTT ciphertext uint64[2][2][D] */
+    uint8_t *response;       /* sp_response_bytes() bytes */
+    uint64_t response_len;
+    int32_t status;          /* out: SP_OK or an error code */
+} sp_request;
+
+/* ------------------------------------------------------------------ */
+/* Context (replaces gen_twiddles_gpu / checkLast, gpu-pir/host.cu:79-138) */
+int sp_ctx_create(const sp_params *params, uint64_t hbm_budget_bytes, sp_ctx **out);
+int sp_ctx_destroy(sp_ctx *ctx);
+int sp_last_error(char *buf, size_t len);
+int sp_response_bytes(const sp_ctx *ctx, uint64_t *bytes);
+int sp_hbm_used(const sp_ctx *ctx, uint64_t *bytes);
+
+/* ------------------------------------------------------------------ */
+/* Databases.  Record i = row * 2^nu2 + col; a record is n*n plaintext
+ * polynomials of D coefficients in [0, p), one byte each. */
+
+/* Encode plaintext records into the device CRT-NTT image (the encoder the
+ * reference leaves as a note, gpu-pir/optplan.md:80-84). */
+int sp_db_load_plain(sp_ctx *ctx, int32_t db_id, const uint8_t *records, uint64_t n_records,
+                     int32_t nu1, int32_t nu2);
+/* Load an image already in NTT form: uint32 planes [n*n][2^nu2][2^nu1][2][D]
+ * (the reference's Database<Poly<uint32_t>> layout col[c].row[r].crt[k],
+ * gpu-pir/structures.cuh:200-210, load_db gpu-pir/db_mul_test.cu:23-34). */
+int sp_db_load_ntt(sp_ctx *ctx, int32_t db_id, const uint32_t *planes, int32_t nu1, int32_t nu2);
+int sp_db_unload(sp_ctx *ctx, int32_t db_id);
+
+/* ------------------------------------------------------------------ */
+/* Client public parameters, uint64 CRT form (load_polys(.., crt_form, montgomery)
+ * gpu-pir/host.cu:216-249; PublicParameters gpu-pir/structures.cuh:173-177):
+ *   exp_left  [n_left][2][t_exp_left][2][D]
+ *   exp_right [n_right][2][t_exp_right][2][D]
+ *   conv      [2][2*t_conv][2][D]
+ *   pack      [n][n+1][t_conv][2][D]                                  */
+int sp_client_set_keys(sp_ctx *ctx, int32_t client_id, const uint64_t *exp_left, int32_t n_left,
+                       const uint64_t *exp_right, int32_t n_right, const uint64_t *conv,
+                       const uint64_t *pack);
+int sp_client_evict(sp_ctx *ctx, int32_t client_id);
+
+/* ------------------------------------------------------------------ */
+/* Answering (the flow of the reference's test main()s, wired end to end):
+ * expansion -> Regev->GSW -> G - C -> first-dimension multiply -> fold ->
+ * pack -> modulus switch -> serialise. */
+int sp_answer(sp_ctx *ctx, int32_t client_id, int32_t db_id, const uint64_t *query,
+              uint8_t *response, uint64_t response_len);
+int sp_answer_batch(sp_ctx *ctx, int32_t count, sp_request *reqs);
+
+/* Device-resident answering for throughput measurement: stage queries into
+ * workspace slots (host->device), run the answer on resident data, fetch
+ * responses (device->host) separately.  sp_answer / sp_answer_batch use the
+ * same slots and consume any staged queries. */
+int sp_stage_query(sp_ctx *ctx, int32_t slot, int32_t client_id, int32_t db_id, const uint64_t *query);
+int sp_run_staged(sp_ctx *ctx, int32_t count);
+int sp_fetch_response(sp_ctx *ctx, int32_t slot, uint8_t *response, uint64_t response_len);
+/* Run the staged queries `iters` times back to back on the context's stream,
+ * timed with CUDA events on that stream; ms per run of all `count` queries. */
+int sp_time_staged(sp_ctx *ctx, int32_t count, int32_t iters, double *ms_per_run);
+
+int sp_stats(sp_ctx *ctx, sp_stats_out *out);
+int sp_stats_reset(sp_ctx *ctx);
+/* Time `iters` launches of the first-dimension multiply of db_id on the
+ * selectors staged in slots [0, nq) with CUDA events; ms per launch. */
+int sp_time_db_mul(sp_ctx *ctx, int32_t db_id, int32_t nq, int32_t iters, double *ms_per_launch);
+
+/* ------------------------------------------------------------------ */
+/* Stage entry points on host buffers, for parity tests.                */
+
+/* raw -> CRT NTT form (NTT_R, gpu-pir/ntt_28bit.cuh:251-270). */
+int sp_ntt_fwd(sp_ctx *ctx, const uint64_t *raw, uint64_t *crt, uint64_t count);
+/* CRT NTT form -> raw: INTT + inverse CRT (INTT_R + from_ntt_regs,
+ * gpu-pir/ntt_28bit.cuh:292-314, gpu-pir/gadget.cuh:8-24). */
+int sp_ntt_inv(sp_ctx *ctx, const uint64_t *crt, uint64_t *raw, uint64_t count);
+/* raw x -> x^t (automorph, gpu-pir/automorph.cuh:54-61). */
+int sp_automorph(sp_ctx *ctx, const uint64_t *raw, uint64_t *out, uint64_t count, uint32_t t);
+/* Coefficient expansion with the client's keys (coefficient_expansion_r,
+ * gpu-pir/expansion.cuh:222-259): `rounds` rounds (0 = all g rounds for
+ * the shape) of query uint64[2][2][D] into out uint64[2^rounds][2][2][D]. */
+int sp_expand(sp_ctx *ctx, int32_t client_id, const uint64_t *query, int32_t nu1, int32_t nu2,
+              int32_t rounds, uint64_t *out);
+/* Regev -> GSW with the client's conversion key (the slot
+ * PublicParameters.conversion, gpu-pir/structures.cuh:176):
+ *   regev uint64[nu2*t_gsw][2][2][D] -> gsw uint64[nu2][2][2*t_gsw][2][D] */
+int sp_regev_to_gsw(sp_ctx *ctx, int32_t client_id, const uint64_t *regev, int32_t nu2, uint64_t *gsw);
+/* G - C for `count` GSW ciphertexts [2][2*t_gsw][2][D] (v_folding_neg). */
+int sp_gsw_neg(sp_ctx *ctx, const uint64_t *gsw, int32_t count, uint64_t *neg);
+/* First-dimension multiply (db_mul_kernel, gpu-pir/db_mul.cuh:26-70):
+ *   sel uint64[2^nu1][2][2][D] -> acc uint64[n*n][2^nu2][2][2][D] */
+int sp_db_mul(sp_ctx *ctx, int32_t db_id, const uint64_t *sel, uint64_t *acc);
+/* Fold (FOLD_CIPHERTEXTS, gpu-pir/folding.cuh:45-65) of T instances:
+ *   cts uint64[T][2^nu2][2][D] raw, gsw uint64[nu2][2][2*t_gsw][2][D]
+ *   -> out uint64[T][2][D] raw.  (G - C is derived, not passed.) */
+int sp_fold(sp_ctx *ctx, const uint64_t *cts, const uint64_t *gsw, int32_t T, int32_t nu2, uint64_t *out);
+/* Pack n*n raw ciphertexts uint64[n*n][2][D] with the client's packing
+ * keys, modulus-switch and serialise into `response`. */
+int sp_pack(sp_ctx *ctx, int32_t client_id, const uint64_t *cts, uint8_t *response, uint64_t response_len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPIRALPIR_H */
