@@ -57,7 +57,7 @@ def dist_info():
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms."""
 
     def __init__(self, index: int):
         self.index = index
@@ -68,7 +68,7 @@ class ClockSampler:
     def start(self):
         cmd = ["nvidia-smi", "-i", str(self.index),
                "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active",
-               "--format=csv,noheader,nounits", "-lms", "200"]
+               "--format=csv,noheader,nounits", "-lms", "50"]
         try:
             self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
@@ -260,6 +260,11 @@ def run_gpu(args, rank, world, local):
     ms = gpu.time_staged(batch, args.steps)
     st = gpu.stats()
     launches_per_answer = st["launches"] / max(1, args.steps)
+    # per-stage split: CUDA events inside three more staged runs
+    gpu.stats_reset()
+    for _ in range(3):
+        gpu.run_staged(batch)
+    split = gpu.stats()
     # first-dimension multiply alone (roofline): CUDA events around its launches
     mul_ms = gpu.time_db_mul(1, batch, max(args.steps, 5))
     # end to end through the public API (host buffers)
@@ -307,7 +312,7 @@ def run_gpu(args, rank, world, local):
                          "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                          "algorithmic_bytes_per_launch": algo_bytes, "launch_ms": mul_ms,
                          "traffic": traffic},
-            "stages_ms": {k[3:]: st[k] / max(1, args.steps) for k in
+            "stages_ms": {k[3:]: split[k] / 3 for k in
                           ("ms_expand", "ms_convert", "ms_db_mul", "ms_fold", "ms_pack", "ms_total")},
             "gpu_launches": int(st["launches"]), "launches_per_answer": launches_per_answer,
             "batched": batched, "clocks": clk, "db_load_s": load_s, "decoded_ok": ok}
