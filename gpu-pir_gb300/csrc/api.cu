@@ -11,6 +11,7 @@
 
 #include "../../include/spiralpir.h"
 #include "answer.cuh"
+#include "ctx_view.h"
 
 using namespace sp;
 
@@ -1047,3 +1048,19 @@ int sp_pack(sp_ctx *c, int32_t client_id, const uint64_t *cts, uint8_t *response
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------ internal accessors
+namespace sp {
+
+int ctx_view(sp_ctx *c, CtxView *out) {
+    if (!c || !out) return fail(SP_ERR_INVALID, "NULL argument");
+    out->st = c->st;
+    out->tw = c->d_tw;
+    out->params = c->sp;
+    out->mu = &c->mu;
+    return SP_OK;
+}
+
+int set_last_error(int code, const char *msg) { return fail(code, msg); }
+
+}  // namespace sp

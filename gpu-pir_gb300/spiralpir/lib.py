@@ -84,6 +84,7 @@ _SIGS = {
     "sp_gsw_neg": [_P, _P, _I, _P],
     "sp_db_mul": [_P, _I, _P, _P],
     "sp_fold": [_P, _P, _P, _I, _I, _P],
+    "sp_fold_noalloc": [_P, _P, _P, _I, _I, _P],
     "sp_pack": [_P, _I, _P, _P, _U64],
 }
 
@@ -282,6 +283,15 @@ class SpiralGPU:
         T = c.size // ((1 << nu2) * 2 * D)
         out = np.empty((T, 2, D), dtype=np.uint64)
         _check(self.lib.sp_fold(self.h, _ptr(c), _ptr(g), T, nu2, _ptr(out)))
+        return out
+
+    def fold_noalloc(self, cts: np.ndarray, gsw: np.ndarray, nu2: int) -> np.ndarray:
+        """sp_fold without device allocation (fixed library-owned scratch)."""
+        c = _u64(cts)
+        g = _u64(gsw)
+        T = c.size // ((1 << nu2) * 2 * D)
+        out = np.empty((T, 2, D), dtype=np.uint64)
+        _check(self.lib.sp_fold_noalloc(self.h, _ptr(c), _ptr(g), T, nu2, _ptr(out)))
         return out
 
     def pack(self, client_id: int, cts: np.ndarray) -> np.ndarray:

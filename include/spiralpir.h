@@ -167,6 +167,19 @@ int sp_db_mul(sp_ctx *ctx, int32_t db_id, const uint64_t *sel, uint64_t *acc);
  *   cts uint64[T][2^nu2][2][D] raw, gsw uint64[nu2][2][2*t_gsw][2][D]
  *   -> out uint64[T][2][D] raw.  (G - C is derived, not passed.) */
 int sp_fold(sp_ctx *ctx, const uint64_t *cts, const uint64_t *gsw, int32_t T, int32_t nu2, uint64_t *out);
+/* Fold without allocating device memory: same inputs, output and result as
+ * sp_fold, for callers that may not call cudaMalloc at that point (inside a
+ * stream capture, under an external allocator, or after a start-up-only
+ * allocation phase).  No counterpart in the reference.  Device storage is a
+ * fixed 8 MiB + 4 KiB array the library declares per GPU, held until the
+ * process exits; inputs needing more than that (T * 2^nu2 * 32 KiB of
+ * ciphertexts plus 24 * nu2 * t_gsw KiB of GSW ciphertexts) are rejected with
+ * SP_ERR_INVALID.  The first call on a device resolves the array's device
+ * address (cudaGetSymbolAddress); make that first call before any stream
+ * capture.  All calls share the one array: calls are serialised by a
+ * process-wide lock and each waits for its own GPU work, since two calls
+ * overlapping on the GPU would race on it. */
+int sp_fold_noalloc(sp_ctx *ctx, const uint64_t *cts, const uint64_t *gsw, int32_t T, int32_t nu2, uint64_t *out);
 /* Pack n*n raw ciphertexts uint64[n*n][2][D] with the client's packing
  * keys, modulus-switch and serialise into `response`. */
 int sp_pack(sp_ctx *ctx, int32_t client_id, const uint64_t *cts, uint8_t *response, uint64_t response_len);
