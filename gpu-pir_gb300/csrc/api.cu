@@ -5,7 +5,11 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <condition_variable>
+#include <deque>
+#include <chrono>
 #include <mutex>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -30,6 +34,12 @@ int fail(int code, const std::string &msg) {
         if (e_ != cudaSuccess)                                                                     \
             return fail(e_ == cudaErrorMemoryAllocation ? SP_ERR_NOMEM : SP_ERR_CUDA,              \
                         std::string(#call) + ": " + cudaGetErrorString(e_));                       \
+    } while (0)
+
+#define TRY(x)                 \
+    do {                       \
+        int rc_ = (x);         \
+        if (rc_) return rc_;   \
     } while (0)
 
 int ceil_log2(uint64_t x) {
@@ -69,28 +79,74 @@ struct Slot {
 
 }  // namespace
 
+namespace {
+
+// One pipeline lane: a stream with its own workspace slots, descriptor
+// arrays, events and pinned response staging.  The synchronous API runs on
+// the main lane; the serving worker owns further lanes so that batches
+// overlap on the GPU.
+struct Lane {
+    cudaStream_t st = nullptr;
+    std::vector<Slot> slots;
+    Shape slot_shape{};
+    QDesc *d_qd = nullptr;       // [cap]
+    QDesc *h_qd = nullptr;       // pinned mirror
+    uint8_t *h_resp = nullptr;   // pinned responses [cap][response bytes]
+    cudaEvent_t ev[6]{};
+    cudaEvent_t done = nullptr;
+    int *d_err = nullptr;
+    int cap = 0;
+    int staged = 0;
+    bool busy = false;                  // serving: a batch is in flight
+    std::vector<uint64_t> tickets;      // serving: tickets of that batch, slot order
+};
+
+struct Pending {
+    uint64_t ticket;
+    int client_id, db_id;
+    std::vector<uint64_t> query;        // copied at submission
+    uint8_t *response;
+    uint64_t response_len;
+};
+
+struct TicketState {
+    int done = 0;
+    int status = 0;
+    uint8_t *response = nullptr;
+};
+
+}  // namespace
+
 struct sp_ctx {
     sp_params p{};
     StageParams sp{};
     int device = 0;
-    cudaStream_t st = nullptr;
+    Lane main;
+    cudaStream_t st = nullptr;      // main.st (stage entry points)
+    int *d_err = nullptr;           // main.d_err
     TwiddleSet *d_tw = nullptr;
     uint32_t *d_neg1 = nullptr;     // [11][2][D] Montgomery form of NTT(x^(-2^r))
-    int *d_err = nullptr;
-    QDesc *d_qd = nullptr;          // [max_batch]
-    QDesc *h_qd = nullptr;          // pinned mirror
-    uint8_t *h_stage = nullptr;     // pinned staging for queries/responses
+    uint8_t *h_stage = nullptr;     // pinned staging for database uploads
     uint64_t stage_bytes = 0;
     std::map<int, Db> dbs;
     std::map<int, Client> clients;
-    std::vector<Slot> slots;
-    Shape slot_shape{};
     uint64_t budget = 0, used = 0;
     uint64_t clock = 0;
     std::mutex mu;
-    cudaEvent_t ev[6]{};
     sp_stats_out stats{};
-    int staged = 0;
+    // multiply variant chosen per (database id, queries in the launch):
+    // 1 = per-query streaming kernel, 2 = batched kernel
+    std::map<std::pair<int, int>, int> mul_choice;
+    int mul_force = 0;          // 0 = autotune, 1/2 = force a variant
+    // serving (continuous batching)
+    std::vector<Lane *> lanes;
+    std::thread worker;
+    std::condition_variable cv;
+    bool serving = false, stopping = false;
+    std::deque<Pending> queue;
+    std::map<uint64_t, TicketState> tickets;
+    uint64_t next_ticket = 1;
+    uint64_t served = 0, batches = 0;
 };
 
 namespace {
@@ -181,27 +237,27 @@ void carve(sp_ctx *c, Slot &sl, const Shape &s) {
 }
 
 // Make sure there are `count` slots big enough for shape `need`.
-int ensure_slots(sp_ctx *c, const Shape &need, int count) {
-    Shape s = c->slot_shape;
+int ensure_slots(sp_ctx *c, Lane &L, const Shape &need, int count) {
+    Shape s = L.slot_shape;
     bool grow = need.nu1 > s.nu1 || need.nu2 > s.nu2 || need.g > s.g;
     s.nu1 = std::max(s.nu1, need.nu1);
     s.nu2 = std::max(s.nu2, need.nu2);
     s.g = std::max(s.g, need.g);
     if (grow) {
-        CU(cudaStreamSynchronize(c->st));
-        for (auto &sl : c->slots) release(c, sl.base, sl.bytes);
-        c->slots.clear();
-        c->staged = 0;
+        CU(cudaStreamSynchronize(L.st));
+        for (auto &sl : L.slots) release(c, sl.base, sl.bytes);
+        L.slots.clear();
+        L.staged = 0;
     }
-    c->slot_shape = s;
+    L.slot_shape = s;
     const uint64_t b = slot_bytes(c, s);
-    while ((int)c->slots.size() < count) {
+    while ((int)L.slots.size() < count) {
         Slot sl;
         int rc = alloc(c, (void **)&sl.base, b);
         if (rc) return rc;
         sl.bytes = b;
         carve(c, sl, s);
-        c->slots.push_back(sl);
+        L.slots.push_back(sl);
     }
     return SP_OK;
 }
@@ -212,6 +268,47 @@ int ensure_staging(sp_ctx *c, uint64_t bytes) {
     c->h_stage = nullptr;
     CU(cudaMallocHost(&c->h_stage, bytes));
     c->stage_bytes = bytes;
+    return SP_OK;
+}
+
+int lane_init(sp_ctx *c, Lane &L, int cap) {
+    L.cap = cap;
+    CU(cudaStreamCreateWithFlags(&L.st, cudaStreamNonBlocking));
+    for (auto &e : L.ev) CU(cudaEventCreate(&e));
+    CU(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming));
+    TRY(alloc(c, (void **)&L.d_err, 16));
+    TRY(alloc(c, (void **)&L.d_qd, sizeof(QDesc) * cap));
+    CU(cudaMallocHost(&L.h_qd, sizeof(QDesc) * cap));
+    memset(L.h_qd, 0, sizeof(QDesc) * cap);
+    CU(cudaMallocHost(&L.h_resp, response_bytes(c->sp) * cap));
+    CU(cudaMemset(L.d_err, 0, 16));
+    return SP_OK;
+}
+
+void lane_free(sp_ctx *c, Lane &L) {
+    if (L.st) cudaStreamSynchronize(L.st);
+    for (auto &sl : L.slots) release(c, sl.base, sl.bytes);
+    L.slots.clear();
+    release(c, L.d_err, 16);
+    release(c, L.d_qd, sizeof(QDesc) * L.cap);
+    L.d_err = nullptr;
+    L.d_qd = nullptr;
+    if (L.h_qd) cudaFreeHost(L.h_qd);
+    if (L.h_resp) cudaFreeHost(L.h_resp);
+    L.h_qd = nullptr;
+    L.h_resp = nullptr;
+    for (auto &e : L.ev)
+        if (e) cudaEventDestroy(e);
+    if (L.done) cudaEventDestroy(L.done);
+    if (L.st) cudaStreamDestroy(L.st);
+    L.st = nullptr;
+}
+
+// Wait for the GPU work of every lane (before freeing keys or databases).
+int sync_all(sp_ctx *c) {
+    if (c->main.st) CU(cudaStreamSynchronize(c->main.st));
+    for (Lane *l : c->lanes)
+        if (l->st) CU(cudaStreamSynchronize(l->st));
     return SP_OK;
 }
 
@@ -241,52 +338,94 @@ int check_client_for(const sp_ctx *c, const Client &cl, const Db &db, int *need_
     return SP_OK;
 }
 
+// Autotuner of the first-dimension multiply: the first time a database is
+// multiplied for `nq` queries in one launch, both variants run once on the
+// (already staged) selectors and the faster, by CUDA events, is kept.
+// Their outputs are identical; the timed runs are overwritten by the real one.
+int choose_mul_variant(sp_ctx *c, Lane &L, int db_id, const Db &db, const QDesc *qd, int nq, int *variant) {
+    if (nq < 2 || !db_mul_batch_supported(db.L)) {
+        *variant = 1;
+        return SP_OK;
+    }
+    if (c->mul_force) {
+        *variant = c->mul_force;
+        return SP_OK;
+    }
+    auto key = std::make_pair(db_id, nq);
+    auto it = c->mul_choice.find(key);
+    if (it != c->mul_choice.end()) {
+        *variant = it->second;
+        return SP_OK;
+    }
+    cudaEvent_t e[3];
+    for (auto &x : e) CU(cudaEventCreate(&x));
+    cudaError_t err = cudaEventRecord(e[0], L.st);
+    if (!err) err = launch_db_mul(db.d, db.L, qd, nq, L.d_err, L.st);
+    if (!err) err = cudaEventRecord(e[1], L.st);
+    if (!err) err = launch_db_mul_batch(db.d, db.L, qd, nq, L.st);
+    if (!err) err = cudaEventRecord(e[2], L.st);
+    if (!err) err = cudaEventSynchronize(e[2]);
+    float a = 0, b = 0;
+    if (!err) err = cudaEventElapsedTime(&a, e[0], e[1]);
+    if (!err) err = cudaEventElapsedTime(&b, e[1], e[2]);
+    for (auto &x : e) cudaEventDestroy(x);
+    if (err) return fail(SP_ERR_CUDA, std::string("multiply autotune: ") + cudaGetErrorString(err));
+    *variant = b < a ? 2 : 1;
+    c->mul_choice[key] = *variant;
+    return SP_OK;
+}
+
 // Run the answer pipeline for queries in slots [0, nq) (descriptors already
 // in c->h_qd / c->d_qd, queries in slot.query32).  Records stage events.
-int run_pipeline(sp_ctx *c, int nq, const std::vector<int> &db_of_slot) {
-    cudaStream_t st = c->st;
+int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot) {
+    cudaStream_t st = L.st;
     const StageParams &sp = c->sp;
     int max_g = 0, max_nu2 = 0, max_items = 0;
     for (int i = 0; i < nq; i++) {
-        max_g = std::max(max_g, c->h_qd[i].g);
-        max_nu2 = std::max(max_nu2, c->h_qd[i].nu2);
-        max_items = std::max(max_items, c->h_qd[i].nu2 * sp.t_gsw);
+        max_g = std::max(max_g, L.h_qd[i].g);
+        max_nu2 = std::max(max_nu2, L.h_qd[i].nu2);
+        max_items = std::max(max_items, L.h_qd[i].nu2 * sp.t_gsw);
     }
     uint64_t launches = 0;
-    CU(cudaEventRecord(c->ev[0], st));
+    CU(cudaEventRecord(L.ev[0], st));
     for (int r = 0; r < max_g; r++) {
-        CU(launch_expand_round(c->d_qd, nq, r, 2 << r, sp, c->d_tw, c->d_neg1, st));
+        CU(launch_expand_round(L.d_qd, nq, r, 2 << r, sp, c->d_tw, c->d_neg1, st));
         launches++;
     }
-    CU(cudaEventRecord(c->ev[1], st));
-    CU(launch_regev_to_gsw(c->d_qd, nq, max_items, sp, c->d_tw, st));
+    CU(cudaEventRecord(L.ev[1], st));
+    CU(launch_regev_to_gsw(L.d_qd, nq, max_items, sp, c->d_tw, st));
     launches++;
-    CU(cudaEventRecord(c->ev[2], st));
+    CU(cudaEventRecord(L.ev[2], st));
     // first-dimension multiply: consecutive slots of the same database share a launch
     uint64_t mul_bytes = 0, mul_calls = 0;
     for (int i = 0; i < nq;) {
         int j = i;
         while (j < nq && db_of_slot[j] == db_of_slot[i]) j++;
         const Db &db = c->dbs.at(db_of_slot[i]);
-        CU(launch_db_mul(db.d, db.L, c->d_qd + i, j - i, c->d_err, st));
+        int variant = 1;
+        TRY(choose_mul_variant(c, L, db_of_slot[i], db, L.d_qd + i, j - i, &variant));
+        if (variant == 2)
+            CU(launch_db_mul_batch(db.d, db.L, L.d_qd + i, j - i, st));
+        else
+            CU(launch_db_mul(db.d, db.L, L.d_qd + i, j - i, L.d_err, st));
         launches++;
         mul_calls++;
         mul_bytes += db.L.words * 8 + (uint64_t)(j - i) * ((uint64_t)db.L.rows * D * 16 +
                                                           (uint64_t)db.L.T * db.L.cols * 4 * D * 4);
         i = j;
     }
-    CU(cudaEventRecord(c->ev[3], st));
-    CU(launch_acc_to_raw(c->d_qd, nq, sp.T * (2 << max_nu2), sp, c->d_tw, st));
+    CU(cudaEventRecord(L.ev[3], st));
+    CU(launch_acc_to_raw(L.d_qd, nq, sp.T * (2 << max_nu2), sp, c->d_tw, st));
     launches++;
     for (int lvl = 0; lvl < max_nu2; lvl++) {
-        CU(launch_fold_level(c->d_qd, nq, lvl, sp.T << (max_nu2 - 1 - lvl), sp, c->d_tw, st));
+        CU(launch_fold_level(L.d_qd, nq, lvl, sp.T << (max_nu2 - 1 - lvl), sp, c->d_tw, st));
         launches++;
     }
-    CU(cudaEventRecord(c->ev[4], st));
-    CU(launch_pack(c->d_qd, nq, sp, c->d_tw, st));
-    CU(launch_bitpack(c->d_qd, nq, sp, response_bytes(sp), st));
+    CU(cudaEventRecord(L.ev[4], st));
+    CU(launch_pack(L.d_qd, nq, sp, c->d_tw, st));
+    CU(launch_bitpack(L.d_qd, nq, sp, response_bytes(sp), st));
     launches += 2;
-    CU(cudaEventRecord(c->ev[5], st));
+    CU(cudaEventRecord(L.ev[5], st));
     c->stats.launches += launches;
     c->stats.db_mul_calls += mul_calls;
     c->stats.db_mul_bytes += mul_bytes;
@@ -294,10 +433,10 @@ int run_pipeline(sp_ctx *c, int nq, const std::vector<int> &db_of_slot) {
     return SP_OK;
 }
 
-int collect_stats(sp_ctx *c) {
+int collect_stats(sp_ctx *c, Lane &L) {
     float ms[5], tot;
-    for (int i = 0; i < 5; i++) CU(cudaEventElapsedTime(&ms[i], c->ev[i], c->ev[i + 1]));
-    CU(cudaEventElapsedTime(&tot, c->ev[0], c->ev[5]));
+    for (int i = 0; i < 5; i++) CU(cudaEventElapsedTime(&ms[i], L.ev[i], L.ev[i + 1]));
+    CU(cudaEventElapsedTime(&tot, L.ev[0], L.ev[5]));
     c->stats.ms_expand += ms[0];
     c->stats.ms_convert += ms[1];
     c->stats.ms_db_mul += ms[2];
@@ -307,12 +446,12 @@ int collect_stats(sp_ctx *c) {
     return SP_OK;
 }
 
-int check_device_err(sp_ctx *c) {
+int check_device_err(sp_ctx *c, Lane &L) {
     int h = 0;
-    CU(cudaMemcpyAsync(&h, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->st));
-    CU(cudaStreamSynchronize(c->st));
+    CU(cudaMemcpyAsync(&h, L.d_err, sizeof(int), cudaMemcpyDeviceToHost, L.st));
+    CU(cudaStreamSynchronize(L.st));
     if (h) {
-        CU(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
+        CU(cudaMemsetAsync(L.d_err, 0, sizeof(int), L.st));
         return fail(SP_ERR_DEVICE, "a device-side bounded wait ran out (code " + std::to_string(h) + ")");
     }
     return SP_OK;
@@ -332,16 +471,12 @@ struct Tmp {
     template <typename T> T *as() const { return (T *)p; }
 };
 
-#define TRY(x)                 \
-    do {                       \
-        int rc_ = (x);         \
-        if (rc_) return rc_;   \
-    } while (0)
-
 }  // namespace
 
 // ===================================================================== API
 extern "C" {
+
+int sp_serve_stop(sp_ctx *c);
 
 int sp_last_error(char *buf, size_t len) {
     if (!buf || !len) return SP_ERR_INVALID;
@@ -374,18 +509,13 @@ int sp_ctx_create(const sp_params *params, uint64_t hbm_budget_bytes, sp_ctx **o
         return rc;
     };
     if (cudaGetDevice(&c->device) != cudaSuccess) return bail(fail(SP_ERR_CUDA, "cudaGetDevice failed"));
-    if (cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking) != cudaSuccess)
-        return bail(fail(SP_ERR_CUDA, "cudaStreamCreate failed"));
-    for (auto &e : c->ev)
-        if (cudaEventCreate(&e) != cudaSuccess) return bail(fail(SP_ERR_CUDA, "cudaEventCreate failed"));
-    int rc = alloc(c, (void **)&c->d_tw, sizeof(TwiddleSet));
-    if (!rc) rc = alloc(c, (void **)&c->d_neg1, (uint64_t)LOGD * 2 * D * 4);
-    if (!rc) rc = alloc(c, (void **)&c->d_err, 16);
-    if (!rc) rc = alloc(c, (void **)&c->d_qd, sizeof(QDesc) * params->max_batch);
+    int rc = lane_init(c, c->main, params->max_batch);
     if (rc) return bail(rc);
-    if (cudaMallocHost(&c->h_qd, sizeof(QDesc) * params->max_batch) != cudaSuccess)
-        return bail(fail(SP_ERR_NOMEM, "cudaMallocHost failed"));
-    memset(c->h_qd, 0, sizeof(QDesc) * params->max_batch);
+    c->st = c->main.st;
+    c->d_err = c->main.d_err;
+    rc = alloc(c, (void **)&c->d_tw, sizeof(TwiddleSet));
+    if (!rc) rc = alloc(c, (void **)&c->d_neg1, (uint64_t)LOGD * 2 * D * 4);
+    if (rc) return bail(rc);
     // constant tables
     std::vector<TwiddleSet> tw(1);
     build_twiddles_host(tw.data());
@@ -405,8 +535,7 @@ int sp_ctx_create(const sp_params *params, uint64_t hbm_budget_bytes, sp_ctx **o
             }
         }
     if (cudaMemcpy(c->d_tw, tw.data(), sizeof(TwiddleSet), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemcpy(c->d_neg1, neg1.data(), neg1.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemset(c->d_err, 0, 16) != cudaSuccess)
+        cudaMemcpy(c->d_neg1, neg1.data(), neg1.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)
         return bail(fail(SP_ERR_CUDA, "constant upload failed"));
     *out = c;
     return SP_OK;
@@ -414,19 +543,14 @@ int sp_ctx_create(const sp_params *params, uint64_t hbm_budget_bytes, sp_ctx **o
 
 int sp_ctx_destroy(sp_ctx *c) {
     if (!c) return SP_OK;
-    if (c->st) cudaStreamSynchronize(c->st);
+    sp_serve_stop(c);
+    sync_all(c);
     for (auto &kv : c->dbs) release(c, kv.second.d, kv.second.bytes);
     for (auto &kv : c->clients) release(c, kv.second.keys, kv.second.bytes);
-    for (auto &sl : c->slots) release(c, sl.base, sl.bytes);
+    lane_free(c, c->main);
     release(c, c->d_tw, sizeof(TwiddleSet));
     release(c, c->d_neg1, (uint64_t)LOGD * 2 * D * 4);
-    release(c, c->d_err, 16);
-    release(c, c->d_qd, sizeof(QDesc) * c->p.max_batch);
-    if (c->h_qd) cudaFreeHost(c->h_qd);
     if (c->h_stage) cudaFreeHost(c->h_stage);
-    for (auto &e : c->ev)
-        if (e) cudaEventDestroy(e);
-    if (c->st) cudaStreamDestroy(c->st);
     delete c;
     return SP_OK;
 }
@@ -459,7 +583,7 @@ static int db_check_shape(sp_ctx *c, int nu1, int nu2) {
 static int db_alloc(sp_ctx *c, int db_id, int nu1, int nu2, Db &db) {
     TRY(db_check_shape(c, nu1, nu2));
     if (c->dbs.count(db_id)) {
-        CU(cudaStreamSynchronize(c->st));
+        TRY(sync_all(c));
         release(c, c->dbs[db_id].d, c->dbs[db_id].bytes);
         c->dbs.erase(db_id);
     }
@@ -540,7 +664,7 @@ int sp_db_unload(sp_ctx *c, int32_t db_id) {
     std::lock_guard<std::mutex> lk(c->mu);
     auto it = c->dbs.find(db_id);
     if (it == c->dbs.end()) return fail(SP_ERR_NOT_FOUND, "unknown database id");
-    CU(cudaStreamSynchronize(c->st));
+    TRY(sync_all(c));
     release(c, it->second.d, it->second.bytes);
     c->dbs.erase(it);
     return SP_OK;
@@ -569,7 +693,7 @@ int sp_client_set_keys(sp_ctx *c, int32_t client_id, const uint64_t *exp_left, i
     const uint64_t wl = (uint64_t)n_left * 2 * s.t_left * P, wr = (uint64_t)n_right * 2 * s.t_right * P;
     const uint64_t wc = 2ull * 2 * s.t_conv * P, wp = (uint64_t)s.n * (s.n + 1) * s.t_conv * P;
     const uint64_t words = wl + wr + wc + wp;
-    CU(cudaStreamSynchronize(c->st));
+    TRY(sync_all(c));
     auto old = c->clients.find(client_id);
     if (old != c->clients.end()) {
         release(c, old->second.keys, old->second.bytes);
@@ -616,7 +740,7 @@ int sp_client_evict(sp_ctx *c, int32_t client_id) {
     std::lock_guard<std::mutex> lk(c->mu);
     auto it = c->clients.find(client_id);
     if (it == c->clients.end()) return fail(SP_ERR_NOT_FOUND, "unknown client id");
-    CU(cudaStreamSynchronize(c->st));
+    TRY(sync_all(c));
     release(c, it->second.keys, it->second.bytes);
     c->clients.erase(it);
     return SP_OK;
@@ -626,8 +750,8 @@ int sp_client_evict(sp_ctx *c, int32_t client_id) {
 // Validate requests and fill slots [0, n) with descriptors (queries copied
 // in from host memory).  Requests are ordered by database so that each
 // database's multiply is one launch.
-static int prepare(sp_ctx *c, int n, sp_request *reqs, std::vector<int> &order, std::vector<int> &db_of_slot) {
-    if (n < 1 || n > c->p.max_batch) return fail(SP_ERR_INVALID, "batch size out of range");
+static int prepare(sp_ctx *c, Lane &L, int n, sp_request *reqs, std::vector<int> &order, std::vector<int> &db_of_slot) {
+    if (n < 1 || n > L.cap) return fail(SP_ERR_INVALID, "batch size out of range");
     Shape need{};
     for (int i = 0; i < n; i++) {
         sp_request &r = reqs[i];
@@ -644,45 +768,46 @@ static int prepare(sp_ctx *c, int n, sp_request *reqs, std::vector<int> &order, 
         need.nu2 = std::max(need.nu2, s.nu2);
         need.g = std::max(need.g, s.g);
     }
-    TRY(ensure_slots(c, need, n));
+    TRY(ensure_slots(c, L, need, n));
     order.resize(n);
     for (int i = 0; i < n; i++) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return reqs[a].db_id < reqs[b].db_id; });
     db_of_slot.resize(n);
     for (int k = 0; k < n; k++) {
         sp_request &r = reqs[order[k]];
-        Slot &sl = c->slots[k];
+        Slot &sl = L.slots[k];
         Client &cl = c->clients[r.client_id];
         cl.stamp = ++c->clock;
         fill_desc(c, sl.q, cl, c->dbs[r.db_id]);
         sl.client = r.client_id;
         sl.db = r.db_id;
-        c->h_qd[k] = sl.q;
+        L.h_qd[k] = sl.q;
         db_of_slot[k] = r.db_id;
-        CU(cudaMemcpyAsync(sl.query64, r.query, 4ull * D * 8, cudaMemcpyHostToDevice, c->st));
-        CU(launch_narrow(sl.query64, sl.query32, 4, false, c->st));   // 2 rows x 2 primes
+        CU(cudaMemcpyAsync(sl.query64, r.query, 4ull * D * 8, cudaMemcpyHostToDevice, L.st));
+        CU(launch_narrow(sl.query64, sl.query32, 4, false, L.st));   // 2 rows x 2 primes
     }
-    CU(cudaMemcpyAsync(c->d_qd, c->h_qd, sizeof(QDesc) * n, cudaMemcpyHostToDevice, c->st));
+    CU(cudaMemcpyAsync(L.d_qd, L.h_qd, sizeof(QDesc) * n, cudaMemcpyHostToDevice, L.st));
     return SP_OK;
 }
 
 int sp_answer_batch(sp_ctx *c, int32_t count, sp_request *reqs) {
     if (!c || !reqs) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
+    Lane &L = c->main;
     std::vector<int> order, dbs;
-    int rc = prepare(c, count, reqs, order, dbs);
-    if (!rc) rc = run_pipeline(c, count, dbs);
-    if (!rc) {
-        const uint64_t rb = response_bytes(c->sp);
-        for (int k = 0; k < count && !rc; k++) {
-            cudaError_t e = cudaMemcpyAsync(reqs[order[k]].response, c->slots[k].q.resp, rb,
-                                            cudaMemcpyDeviceToHost, c->st);
-            if (e != cudaSuccess) rc = fail(SP_ERR_CUDA, std::string("response copy: ") + cudaGetErrorString(e));
-        }
+    int rc = prepare(c, L, count, reqs, order, dbs);
+    if (!rc) rc = run_pipeline(c, L, count, dbs);
+    const uint64_t rb = response_bytes(c->sp);
+    for (int k = 0; k < count && !rc; k++) {
+        cudaError_t e = cudaMemcpyAsync(L.h_resp + k * rb, L.slots[k].q.resp, rb, cudaMemcpyDeviceToHost, L.st);
+        if (e != cudaSuccess) rc = fail(SP_ERR_CUDA, std::string("response copy: ") + cudaGetErrorString(e));
     }
-    if (!rc) rc = check_device_err(c);
-    if (!rc) rc = collect_stats(c);
-    c->staged = 0;
+    if (!rc) rc = check_device_err(c, L);
+    if (!rc) {
+        for (int k = 0; k < count; k++) memcpy(reqs[order[k]].response, L.h_resp + k * rb, rb);
+        rc = collect_stats(c, L);
+    }
+    L.staged = 0;
     for (int i = 0; i < count; i++) reqs[i].status = rc;
     return rc;
 }
@@ -696,60 +821,63 @@ int sp_answer(sp_ctx *c, int32_t client_id, int32_t db_id, const uint64_t *query
 int sp_stage_query(sp_ctx *c, int32_t slot, int32_t client_id, int32_t db_id, const uint64_t *query) {
     if (!c || !query) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
-    if (slot < 0 || slot >= c->p.max_batch) return fail(SP_ERR_INVALID, "slot out of range");
+    if (slot < 0 || slot >= c->main.cap) return fail(SP_ERR_INVALID, "slot out of range");
     auto ci = c->clients.find(client_id);
     auto di = c->dbs.find(db_id);
     if (ci == c->clients.end() || di == c->dbs.end()) return fail(SP_ERR_NOT_FOUND, "unknown client or database");
     int nl, nr;
     TRY(check_client_for(c, ci->second, di->second, &nl, &nr));
-    TRY(ensure_slots(c, shape_of(c, di->second.L.nu1, di->second.L.nu2), slot + 1));
-    Slot &sl = c->slots[slot];
+    Lane &L = c->main;
+    TRY(ensure_slots(c, L, shape_of(c, di->second.L.nu1, di->second.L.nu2), slot + 1));
+    Slot &sl = L.slots[slot];
     fill_desc(c, sl.q, ci->second, di->second);
     sl.client = client_id;
     sl.db = db_id;
-    c->h_qd[slot] = sl.q;
-    CU(cudaMemcpyAsync(sl.query64, query, 4ull * D * 8, cudaMemcpyHostToDevice, c->st));
-    CU(launch_narrow(sl.query64, sl.query32, 4, false, c->st));   // 2 rows x 2 primes
-    CU(cudaMemcpyAsync(c->d_qd + slot, &c->h_qd[slot], sizeof(QDesc), cudaMemcpyHostToDevice, c->st));
-    CU(cudaStreamSynchronize(c->st));
-    c->staged = std::max(c->staged, slot + 1);
+    L.h_qd[slot] = sl.q;
+    CU(cudaMemcpyAsync(sl.query64, query, 4ull * D * 8, cudaMemcpyHostToDevice, L.st));
+    CU(launch_narrow(sl.query64, sl.query32, 4, false, L.st));   // 2 rows x 2 primes
+    CU(cudaMemcpyAsync(L.d_qd + slot, &L.h_qd[slot], sizeof(QDesc), cudaMemcpyHostToDevice, L.st));
+    CU(cudaStreamSynchronize(L.st));
+    L.staged = std::max(L.staged, slot + 1);
     return SP_OK;
 }
 
 int sp_run_staged(sp_ctx *c, int32_t count) {
     if (!c) return fail(SP_ERR_INVALID, "NULL context");
     std::lock_guard<std::mutex> lk(c->mu);
-    if (count < 1 || count > c->staged) return fail(SP_ERR_INVALID, "count exceeds staged queries");
+    Lane &L = c->main;
+    if (count < 1 || count > L.staged) return fail(SP_ERR_INVALID, "count exceeds staged queries");
     std::vector<int> dbs(count);
     for (int k = 0; k < count; k++) {
-        dbs[k] = c->slots[k].db;
-        if (!c->dbs.count(dbs[k]) || !c->clients.count(c->slots[k].client))
+        dbs[k] = L.slots[k].db;
+        if (!c->dbs.count(dbs[k]) || !c->clients.count(L.slots[k].client))
             return fail(SP_ERR_NOT_FOUND, "staged query refers to an unloaded database or client");
     }
     for (int k = 1; k < count; k++)
         if (dbs[k] < dbs[k - 1]) return fail(SP_ERR_INVALID, "stage slots in database order");
-    TRY(run_pipeline(c, count, dbs));
-    TRY(check_device_err(c));
-    return collect_stats(c);
+    TRY(run_pipeline(c, L, count, dbs));
+    TRY(check_device_err(c, L));
+    return collect_stats(c, L);
 }
 
 int sp_time_staged(sp_ctx *c, int32_t count, int32_t iters, double *ms_per_run) {
     if (!c || !ms_per_run) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
-    if (count < 1 || count > c->staged || iters < 1) return fail(SP_ERR_INVALID, "count/iters out of range");
+    Lane &L = c->main;
+    if (count < 1 || count > L.staged || iters < 1) return fail(SP_ERR_INVALID, "count/iters out of range");
     std::vector<int> dbs(count);
-    for (int k = 0; k < count; k++) dbs[k] = c->slots[k].db;
+    for (int k = 0; k < count; k++) dbs[k] = L.slots[k].db;
     cudaEvent_t a, b;
     CU(cudaEventCreate(&a));
     CU(cudaEventCreate(&b));
     int rc = SP_OK;
     float tot = 0;
-    if (cudaEventRecord(a, c->st) != cudaSuccess) rc = fail(SP_ERR_CUDA, "event record failed");
-    for (int i = 0; i < iters && !rc; i++) rc = run_pipeline(c, count, dbs);
-    if (!rc && cudaEventRecord(b, c->st) != cudaSuccess) rc = fail(SP_ERR_CUDA, "event record failed");
-    if (!rc) rc = check_device_err(c);
+    if (cudaEventRecord(a, L.st) != cudaSuccess) rc = fail(SP_ERR_CUDA, "event record failed");
+    for (int i = 0; i < iters && !rc; i++) rc = run_pipeline(c, L, count, dbs);
+    if (!rc && cudaEventRecord(b, L.st) != cudaSuccess) rc = fail(SP_ERR_CUDA, "event record failed");
+    if (!rc) rc = check_device_err(c, L);
     if (!rc && cudaEventElapsedTime(&tot, a, b) != cudaSuccess) rc = fail(SP_ERR_CUDA, "event time failed");
-    if (!rc) rc = collect_stats(c);   // stage split of the last run only
+    if (!rc) rc = collect_stats(c, L);   // stage split of the last run only
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     if (!rc) *ms_per_run = tot / iters;
@@ -759,11 +887,20 @@ int sp_time_staged(sp_ctx *c, int32_t count, int32_t iters, double *ms_per_run) 
 int sp_fetch_response(sp_ctx *c, int32_t slot, uint8_t *response, uint64_t response_len) {
     if (!c || !response) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
-    if (slot < 0 || slot >= (int)c->slots.size()) return fail(SP_ERR_INVALID, "slot out of range");
+    Lane &L = c->main;
+    if (slot < 0 || slot >= (int)L.slots.size()) return fail(SP_ERR_INVALID, "slot out of range");
     const uint64_t rb = response_bytes(c->sp);
     if (response_len < rb) return fail(SP_ERR_INVALID, "response buffer too small");
-    CU(cudaMemcpyAsync(response, c->slots[slot].q.resp, rb, cudaMemcpyDeviceToHost, c->st));
-    CU(cudaStreamSynchronize(c->st));
+    CU(cudaMemcpyAsync(response, L.slots[slot].q.resp, rb, cudaMemcpyDeviceToHost, L.st));
+    CU(cudaStreamSynchronize(L.st));
+    return SP_OK;
+}
+
+int sp_set_db_mul_variant(sp_ctx *c, int32_t variant) {
+    if (!c) return fail(SP_ERR_INVALID, "NULL context");
+    if (variant < 0 || variant > 2) return fail(SP_ERR_INVALID, "variant must be 0 (auto), 1 or 2");
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->mul_force = variant;
     return SP_OK;
 }
 
@@ -784,17 +921,18 @@ int sp_stats_reset(sp_ctx *c) {
 int sp_time_db_mul(sp_ctx *c, int32_t db_id, int32_t nq, int32_t iters, double *ms_per_launch) {
     if (!c || !ms_per_launch) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
+    Lane &L = c->main;
     auto di = c->dbs.find(db_id);
     if (di == c->dbs.end()) return fail(SP_ERR_NOT_FOUND, "unknown database id");
-    if (nq < 1 || nq > c->staged || iters < 1) return fail(SP_ERR_INVALID, "nq/iters out of range");
+    if (nq < 1 || nq > L.staged || iters < 1) return fail(SP_ERR_INVALID, "nq/iters out of range");
     for (int k = 0; k < nq; k++)
-        if (c->slots[k].db != db_id) return fail(SP_ERR_INVALID, "staged slots must query this database");
-    CU(cudaEventRecord(c->ev[0], c->st));
-    for (int i = 0; i < iters; i++) CU(launch_db_mul(di->second.d, di->second.L, c->d_qd, nq, c->d_err, c->st));
-    CU(cudaEventRecord(c->ev[1], c->st));
-    TRY(check_device_err(c));
+        if (L.slots[k].db != db_id) return fail(SP_ERR_INVALID, "staged slots must query this database");
+    CU(cudaEventRecord(L.ev[0], L.st));
+    for (int i = 0; i < iters; i++) CU(launch_db_mul(di->second.d, di->second.L, L.d_qd, nq, L.d_err, L.st));
+    CU(cudaEventRecord(L.ev[1], L.st));
+    TRY(check_device_err(c, L));
     float ms = 0;
-    CU(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+    CU(cudaEventElapsedTime(&ms, L.ev[0], L.ev[1]));
     *ms_per_launch = ms / iters;
     return SP_OK;
 }
@@ -983,7 +1121,7 @@ int sp_db_mul(sp_ctx *c, int32_t db_id, const uint64_t *sel, uint64_t *acc) {
     CU(launch_db_mul(di->second.d, L, qd.as<QDesc>(), 1, c->d_err, c->st));
     CU(launch_widen(o.as<uint32_t>(), w.as<uint64_t>(), acc_words / D, false, c->st));
     CU(cudaMemcpyAsync(acc, w.p, acc_words * 8, cudaMemcpyDeviceToHost, c->st));
-    TRY(check_device_err(c));
+    TRY(check_device_err(c, c->main));
     return SP_OK;
 }
 
@@ -1064,3 +1202,214 @@ int ctx_view(sp_ctx *c, CtxView *out) {
 int set_last_error(int code, const char *msg) { return fail(code, msg); }
 
 }  // namespace sp
+
+// ======================================================== serving loop
+// Continuous batching: sp_submit queues a request (the query is copied); a
+// worker thread launches the queued requests, up to max_batch at a time, on
+// whichever lane is free, so a batch admitted while others run overlaps
+// with them on the GPU.  Lanes own their slots (device workspace sized under
+// the HBM budget), their stream and pinned response staging; a finished
+// lane's responses are copied to the callers' buffers and their tickets
+// completed.
+namespace {
+
+void complete(sp_ctx *c, uint64_t ticket, int status) {
+    auto it = c->tickets.find(ticket);
+    if (it != c->tickets.end()) {
+        it->second.done = 1;
+        it->second.status = status;
+    }
+}
+
+void finish_lane(sp_ctx *c, Lane &L) {
+    int status = check_device_err(c, L);
+    if (!status) status = collect_stats(c, L);
+    const uint64_t rb = response_bytes(c->sp);
+    for (size_t k = 0; k < L.tickets.size(); k++) {
+        auto it = c->tickets.find(L.tickets[k]);
+        if (it == c->tickets.end()) continue;
+        if (!status) memcpy(it->second.response, L.h_resp + k * rb, rb);
+        complete(c, L.tickets[k], status);
+    }
+    c->served += L.tickets.size();
+    L.tickets.clear();
+    L.busy = false;
+    L.staged = 0;
+}
+
+// Launch up to L.cap queued requests on lane L (lock held).
+void launch_lane(sp_ctx *c, Lane &L) {
+    std::vector<Pending> batch;
+    while (!c->queue.empty() && (int)batch.size() < L.cap) {
+        Pending p = std::move(c->queue.front());
+        c->queue.pop_front();
+        // requests that cannot run complete at once with their error
+        auto ci = c->clients.find(p.client_id);
+        auto di = c->dbs.find(p.db_id);
+        int nl, nr;
+        if (ci == c->clients.end() || di == c->dbs.end()) {
+            fail(SP_ERR_NOT_FOUND, "unknown client or database id");
+            complete(c, p.ticket, SP_ERR_NOT_FOUND);
+            continue;
+        }
+        if (int rc = check_client_for(c, ci->second, di->second, &nl, &nr)) {
+            complete(c, p.ticket, rc);
+            continue;
+        }
+        batch.push_back(std::move(p));
+    }
+    if (batch.empty()) return;
+    std::vector<sp_request> reqs(batch.size());
+    for (size_t k = 0; k < batch.size(); k++)
+        reqs[k] = sp_request{batch[k].client_id, batch[k].db_id, batch[k].query.data(), batch[k].response,
+                             batch[k].response_len, 0};
+    std::vector<int> order, dbs;
+    int rc = prepare(c, L, (int)reqs.size(), reqs.data(), order, dbs);
+    if (!rc) rc = run_pipeline(c, L, (int)reqs.size(), dbs);
+    const uint64_t rb = response_bytes(c->sp);
+    for (size_t k = 0; k < reqs.size() && !rc; k++)
+        if (cudaMemcpyAsync(L.h_resp + k * rb, L.slots[k].q.resp, rb, cudaMemcpyDeviceToHost, L.st) != cudaSuccess)
+            rc = fail(SP_ERR_CUDA, "response copy failed");
+    if (!rc && cudaEventRecord(L.done, L.st) != cudaSuccess) rc = fail(SP_ERR_CUDA, "event record failed");
+    if (rc) {
+        cudaStreamSynchronize(L.st);
+        for (auto &p : batch) complete(c, p.ticket, rc);
+        c->cv.notify_all();
+        return;
+    }
+    L.tickets.clear();
+    for (size_t k = 0; k < order.size(); k++) L.tickets.push_back(batch[order[k]].ticket);
+    L.busy = true;
+    c->batches++;
+}
+
+void serve_worker(sp_ctx *c) {
+    cudaSetDevice(c->device);
+    std::unique_lock<std::mutex> lk(c->mu);
+    for (;;) {
+        bool any_busy = false;
+        for (Lane *L : c->lanes) {
+            if (L->busy && cudaEventQuery(L->done) == cudaSuccess) {
+                finish_lane(c, *L);
+                c->cv.notify_all();
+            }
+            any_busy |= L->busy;
+        }
+        if (!c->queue.empty()) {
+            Lane *free_lane = nullptr;
+            for (Lane *L : c->lanes)
+                if (!L->busy) { free_lane = L; break; }
+            if (free_lane) {
+                launch_lane(c, *free_lane);
+                continue;
+            }
+        }
+        if (c->stopping && c->queue.empty() && !any_busy) break;
+        if (any_busy)
+            c->cv.wait_for(lk, std::chrono::microseconds(50));
+        else
+            c->cv.wait(lk, [&] { return c->stopping || !c->queue.empty(); });
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int sp_serve_start(sp_ctx *c, int32_t lanes) {
+    if (!c) return fail(SP_ERR_INVALID, "NULL context");
+    if (lanes < 1 || lanes > 8) return fail(SP_ERR_INVALID, "lanes must be in [1, 8]");
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (c->serving) return fail(SP_ERR_INVALID, "already serving");
+    for (int i = 0; i < lanes; i++) {
+        Lane *L = new Lane();
+        int rc = lane_init(c, *L, c->p.max_batch);
+        c->lanes.push_back(L);
+        if (rc) {
+            for (Lane *x : c->lanes) {
+                lane_free(c, *x);
+                delete x;
+            }
+            c->lanes.clear();
+            return rc;
+        }
+    }
+    c->serving = true;
+    c->stopping = false;
+    c->worker = std::thread(serve_worker, c);
+    return SP_OK;
+}
+
+int sp_serve_stop(sp_ctx *c) {
+    if (!c) return fail(SP_ERR_INVALID, "NULL context");
+    {
+        std::lock_guard<std::mutex> lk(c->mu);
+        if (!c->serving) return SP_OK;
+        c->stopping = true;
+    }
+    c->cv.notify_all();
+    if (c->worker.joinable()) c->worker.join();
+    std::lock_guard<std::mutex> lk(c->mu);
+    for (Lane *L : c->lanes) {
+        lane_free(c, *L);
+        delete L;
+    }
+    c->lanes.clear();
+    c->serving = false;
+    c->stopping = false;
+    return SP_OK;
+}
+
+int sp_submit(sp_ctx *c, const sp_request *req, uint64_t *ticket) {
+    if (!c || !req || !ticket || !req->query || !req->response) return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    if (!c->serving || c->stopping) return fail(SP_ERR_INVALID, "serving loop not running (sp_serve_start)");
+    if (req->response_len < response_bytes(c->sp)) return fail(SP_ERR_INVALID, "response buffer too small");
+    Pending p;
+    p.ticket = c->next_ticket++;
+    p.client_id = req->client_id;
+    p.db_id = req->db_id;
+    p.query.assign(req->query, req->query + 4ull * D);
+    p.response = req->response;
+    p.response_len = req->response_len;
+    TicketState ts;
+    ts.response = req->response;
+    c->tickets[p.ticket] = ts;
+    *ticket = p.ticket;
+    c->queue.push_back(std::move(p));
+    c->cv.notify_all();
+    return SP_OK;
+}
+
+int sp_poll(sp_ctx *c, uint64_t ticket, int32_t *done, int32_t *status) {
+    if (!c || !done || !status) return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    auto it = c->tickets.find(ticket);
+    if (it == c->tickets.end()) return fail(SP_ERR_NOT_FOUND, "unknown ticket");
+    *done = it->second.done;
+    *status = it->second.status;
+    if (it->second.done) c->tickets.erase(it);
+    return SP_OK;
+}
+
+int sp_wait(sp_ctx *c, uint64_t ticket, int32_t *status) {
+    if (!c || !status) return fail(SP_ERR_INVALID, "NULL argument");
+    std::unique_lock<std::mutex> lk(c->mu);
+    auto it = c->tickets.find(ticket);
+    if (it == c->tickets.end()) return fail(SP_ERR_NOT_FOUND, "unknown ticket");
+    c->cv.wait(lk, [&] { return c->tickets[ticket].done != 0; });
+    *status = c->tickets[ticket].status;
+    c->tickets.erase(ticket);
+    return SP_OK;
+}
+
+int sp_serve_stats(sp_ctx *c, uint64_t *served, uint64_t *batches, uint64_t *queued) {
+    if (!c || !served || !batches || !queued) return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    *served = c->served;
+    *batches = c->batches;
+    *queued = c->queue.size();
+    return SP_OK;
+}
+
+}  // extern "C"

@@ -297,4 +297,123 @@ cudaError_t launch_db_mul(const uint64_t *db, const DbLayout &L, const QDesc *qd
     }
 }
 
+// ------------------------------------------------------- batched multiply
+// Several queries against one database: compute-bound once more than ~3
+// queries share a database word (4 multiply-adds per word per query on the
+// integer pipe), so the database is streamed from global memory directly
+// into registers and each word is reused for BQ queries; CTAs that read the
+// same database stream for different query groups are adjacent in the grid
+// (query group is the fastest grid index) so the stream is fetched from HBM
+// about once and served from L2 to the others.
+//
+// CTA: 256 threads = 32 slots (half of a 64-slot z tile) x 8 pairs of tile
+// words; each thread accumulates 2 words x BQ queries x 4 (row0/row1 x
+// prime) in 64-bit registers, reduced every 128 rows.  Selectors of BQ
+// queries for BR rows are staged in shared memory, double buffered.
+constexpr int BQ = 4;     // queries per CTA
+constexpr int BR = 8;     // rows per selector stage
+
+__global__ void __launch_bounds__(256, 2) k_db_mul_batch(const uint64_t *__restrict__ db, DbLayout L,
+                                                        const QDesc *__restrict__ qd, int nq) {
+    __shared__ __align__(16) uint4 ssel[2][BR][BQ][32];
+    const int qg = blockIdx.x;                  // query group
+    const int tile = blockIdx.y;                // (z tile, z half, column group)
+    const int zh = tile & 1;
+    const int zti = (tile >> 1) % L.nzt, grp = (tile >> 1) / L.nzt;
+    const int zi = threadIdx.x & 31, pair = threadIdx.x >> 5;     // pair of tile words 2*pair, 2*pair+1
+    const int rows = L.rows;
+    const uint64_t *src = db + (uint64_t)(zti * L.ncg + grp) * rows * 16 * 64 + zh * 32 + zi;
+    const int q0 = qg * BQ;
+    const uint32_t *sp[BQ];
+#pragma unroll
+    for (int k = 0; k < BQ; k++) sp[k] = (q0 + k < nq) ? qd[q0 + k].sel : qd[q0].sel;
+    const uint64_t mu0 = ~0ull / QP0, mu1 = ~0ull / QP1;
+
+    // cooperative selector load for rows [r0, r0+BR): BR*BQ*32 uint4 = 1024 -> 4 per thread
+    auto stage = [&](int buf, int r0) {
+#pragma unroll
+        for (int k = 0; k < (BR * BQ * 32) / 256; k++) {
+            const int idx = threadIdx.x + 256 * k;
+            const int zz = idx & 31, qq = (idx >> 5) % BQ, rr = (idx >> 5) / BQ;
+            const uint4 *s = reinterpret_cast<const uint4 *>(sp[qq]) +
+                             ((uint64_t)(r0 + rr) * D + zti * 64 + zh * 32 + zz);
+            ssel[buf][rr][qq][zz] = __ldg(s);
+        }
+    };
+
+    uint64_t acc[2][BQ][4];
+#pragma unroll
+    for (int w = 0; w < 2; w++)
+#pragma unroll
+        for (int q = 0; q < BQ; q++)
+#pragma unroll
+            for (int k = 0; k < 4; k++) acc[w][q][k] = 0;
+
+    stage(0, 0);
+    __syncthreads();
+    for (int r0 = 0, it = 0; r0 < rows; r0 += BR, it++) {
+        const int buf = it & 1;
+        if (r0 + BR < rows) stage(buf ^ 1, r0 + BR);
+        uint64_t dv[BR][2];
+#pragma unroll
+        for (int r = 0; r < BR; r++)
+#pragma unroll
+            for (int w = 0; w < 2; w++) dv[r][w] = __ldg(src + ((uint64_t)(r0 + r) * 16 + 2 * pair + w) * 64);
+#pragma unroll
+        for (int r = 0; r < BR; r++) {
+#pragma unroll
+            for (int q = 0; q < BQ; q++) {
+                const uint4 sv = ssel[buf][r][q][zi];
+#pragma unroll
+                for (int w = 0; w < 2; w++) {
+                    const uint32_t d0 = (uint32_t)dv[r][w], d1 = (uint32_t)(dv[r][w] >> 32);
+                    acc[w][q][0] += (uint64_t)sv.x * d0;
+                    acc[w][q][1] += (uint64_t)sv.y * d1;
+                    acc[w][q][2] += (uint64_t)sv.z * d0;
+                    acc[w][q][3] += (uint64_t)sv.w * d1;
+                }
+            }
+        }
+        if ((r0 + BR) % MUL_REDUCE == 0) {
+#pragma unroll
+            for (int w = 0; w < 2; w++)
+#pragma unroll
+                for (int q = 0; q < BQ; q++) {
+                    acc[w][q][0] = mod_u64_barrett(acc[w][q][0], QP0, mu0);
+                    acc[w][q][1] = mod_u64_barrett(acc[w][q][1], QP1, mu1);
+                    acc[w][q][2] = mod_u64_barrett(acc[w][q][2], QP0, mu0);
+                    acc[w][q][3] = mod_u64_barrett(acc[w][q][3], QP1, mu1);
+                }
+        }
+        __syncthreads();
+    }
+    const int z = zti * 64 + zh * 32 + zi;
+#pragma unroll
+    for (int q = 0; q < BQ; q++) {
+        if (q0 + q >= nq) break;
+        uint32_t *out = qd[q0 + q].acc;
+#pragma unroll
+        for (int w = 0; w < 2; w++) {
+            const int tc = 2 * pair + w;
+            const int t = tc / L.cg, col = grp * L.cg + tc % L.cg;
+            uint32_t *o = out + (((uint64_t)t * L.cols + col) * 4) * D + z;
+            o[0 * D] = mod_u64_barrett(acc[w][q][0], QP0, mu0);
+            o[1 * D] = mod_u64_barrett(acc[w][q][1], QP1, mu1);
+            o[2 * D] = mod_u64_barrett(acc[w][q][2], QP0, mu0);
+            o[3 * D] = mod_u64_barrett(acc[w][q][3], QP1, mu1);
+        }
+    }
+}
+
+bool db_mul_batch_supported(const DbLayout &L) { return L.T * L.cg == 16 && (L.rows % BR) == 0; }
+
+cudaError_t launch_db_mul_batch(const uint64_t *db, const DbLayout &L, const QDesc *qd, int nq, cudaStream_t st) {
+    if (!db_mul_batch_supported(L)) return cudaErrorInvalidValue;
+    if (L.rows > MUL_REDUCE && L.rows % MUL_REDUCE) return cudaErrorInvalidValue;
+    dim3 grid((nq + BQ - 1) / BQ, L.nzt * 2 * L.ncg);
+    if (grid.y > 65535) return cudaErrorInvalidValue;
+    k_db_mul_batch<<<grid, 256, 0, st>>>(db, L, qd, nq);
+    return cudaGetLastError();
+}
+
 }  // namespace sp

@@ -90,5 +90,9 @@ cudaError_t launch_db_import(const uint32_t *planes, const DbLayout &L, uint64_t
 cudaError_t launch_db_mul(const uint64_t *db, const DbLayout &L, const QDesc *qd, int nq, int *err,
                           cudaStream_t st);
 int db_mul_ctas(const DbLayout &L);
+// Same result as launch_db_mul for nq > 1 queries, reading each database
+// word once per group of 4 queries (compute-bound variant).
+bool db_mul_batch_supported(const DbLayout &L);
+cudaError_t launch_db_mul_batch(const uint64_t *db, const DbLayout &L, const QDesc *qd, int nq, cudaStream_t st);
 
 }  // namespace sp

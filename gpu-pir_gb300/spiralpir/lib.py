@@ -73,6 +73,13 @@ _SIGS = {
     "sp_run_staged": [_P, _I],
     "sp_fetch_response": [_P, _I, _P, _U64],
     "sp_time_staged": [_P, _I, _I, ctypes.POINTER(ctypes.c_double)],
+    "sp_set_db_mul_variant": [_P, _I],
+    "sp_serve_start": [_P, _I],
+    "sp_serve_stop": [_P],
+    "sp_submit": [_P, ctypes.POINTER(SpRequest), ctypes.POINTER(_U64)],
+    "sp_poll": [_P, _U64, ctypes.POINTER(_I), ctypes.POINTER(_I)],
+    "sp_wait": [_P, _U64, ctypes.POINTER(_I)],
+    "sp_serve_stats": [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64), ctypes.POINTER(_U64)],
     "sp_stats": [_P, ctypes.POINTER(SpStats)],
     "sp_stats_reset": [_P],
     "sp_time_db_mul": [_P, _I, _I, _I, ctypes.POINTER(ctypes.c_double)],
@@ -216,6 +223,10 @@ class SpiralGPU:
         resp = np.empty(self.response_bytes, dtype=np.uint8)
         _check(self.lib.sp_fetch_response(self.h, slot, _ptr(resp), resp.nbytes))
         return resp
+
+    def set_db_mul_variant(self, variant: int) -> None:
+        """0 = autotune, 1 = per-query streaming multiply, 2 = batched multiply."""
+        _check(self.lib.sp_set_db_mul_variant(self.h, variant))
 
     def stats(self) -> dict:
         s = SpStats()

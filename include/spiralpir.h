@@ -133,6 +133,28 @@ int sp_fetch_response(sp_ctx *ctx, int32_t slot, uint8_t *response, uint64_t res
  * timed with CUDA events on that stream; ms per run of all `count` queries. */
 int sp_time_staged(sp_ctx *ctx, int32_t count, int32_t iters, double *ms_per_run);
 
+/* First-dimension multiply variant for launches with several queries on one
+ * database: 0 = autotune (default: time both once per database and batch
+ * size, keep the faster), 1 = per-query streaming kernel (TMA-fed, HBM-bound),
+ * 2 = batched kernel (each database word read once per 4 queries).  The
+ * result is identical. */
+int sp_set_db_mul_variant(sp_ctx *ctx, int32_t variant);
+/* Serving loop (continuous batching).  sp_serve_start starts a worker thread
+ * with `lanes` pipeline lanes (each its own stream and max_batch workspace
+ * slots).  sp_submit copies the request's query and returns a ticket; the
+ * worker coalesces queued requests into batches of up to max_batch and
+ * launches each on a free lane, so batches admitted while others run overlap
+ * on the GPU.  The response is written to the request's buffer before the
+ * ticket completes (sp_poll / sp_wait); a request that cannot run (unknown
+ * ids, keys that do not cover the database, workspace beyond the HBM
+ * budget) completes with its error status.  sp_serve_stop drains the queue. */
+int sp_serve_start(sp_ctx *ctx, int32_t lanes);
+int sp_serve_stop(sp_ctx *ctx);
+int sp_submit(sp_ctx *ctx, const sp_request *req, uint64_t *ticket);
+int sp_poll(sp_ctx *ctx, uint64_t ticket, int32_t *done, int32_t *status);
+int sp_wait(sp_ctx *ctx, uint64_t ticket, int32_t *status);
+int sp_serve_stats(sp_ctx *ctx, uint64_t *served, uint64_t *batches, uint64_t *queued);
+
 int sp_stats(sp_ctx *ctx, sp_stats_out *out);
 int sp_stats_reset(sp_ctx *ctx);
 /* Time `iters` launches of the first-dimension multiply of db_id on the
