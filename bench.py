@@ -289,10 +289,15 @@ def run_gpu(args, rank, world, local):
             gpu2.stage_query(s, 1, 1, queries[s % len(queries)])
         gpu2.time_staged(args.batched, 1)
         bms = gpu2.time_staged(args.batched, max(2, args.steps // 4))
+        gpu2.stats_reset()
+        gpu2.run_staged(args.batched)
+        bsplit = gpu2.stats()
         rb = gpu2.fetch_response(3 % args.batched)
         assert np.array_equal(cl.decode(rb), recs[idx[3 % args.batched % len(idx)]])
         batched = {"B": args.batched, "queries_per_s": args.batched / (bms / 1e3),
-                   "ms_per_batch": bms, "speedup_vs_single": (args.batched / bms) / (batch / ms)}
+                   "ms_per_batch": bms, "speedup_vs_single": (args.batched / bms) / (batch / ms),
+                   "stages_ms": {k[3:]: bsplit[k] for k in
+                                 ("ms_expand", "ms_convert", "ms_db_mul", "ms_fold", "ms_pack", "ms_total")}}
         gpu2.close()
 
     value = batch * 1e3 / ms * world
@@ -339,7 +344,13 @@ def main():
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--batch", type=int, default=1, help="queries per step (1 = plain single-query path)")
     ap.add_argument("--batched", type=int, default=32, help="also measure a B-query batch (0 to skip)")
+    ap.add_argument("--suite", action="store_true", help="run the other workloads instead (uneven batches, "
+                    "8 GiB database, serving)")
+    ap.add_argument("--skip-8gib", action="store_true", help="suite without the 8 GiB database")
     args = ap.parse_args()
+    if args.suite:
+        run_suite(args)
+        return
     if args.warmup < 3:
         args.warmup = 3
     rank, world, local = dist_info()
@@ -349,6 +360,171 @@ def main():
     if world > 1:
         os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
     run_gpu(args, rank, world, local)
+
+
+
+# --------------------------------------------------------------- suite
+def run_suite(args) -> None:
+    """The other workloads of the answer path, one JSON line each:
+    uneven batches (1 GiB + 64 MiB databases, B in 8/32/64), the 8 GiB
+    database (64 GiB device image) single and B = 16, and the serving loop
+    (three resident databases, 256 clients under an HBM budget with LRU key
+    eviction, seeded Poisson arrivals at swept rates)."""
+    from spiralpir import client as C
+    from spiralpir import params as P
+    from spiralpir.lib import SpiralError, SpiralGPU
+    from spiralpir.serving import Server, poisson_load
+
+    import dataclasses
+
+    p = P.PARAMS
+    # The 8 GiB database (nu2 = 11: 11 fold levels, GSW bits expanded over 8
+    # rounds) leaves too little noise margin with 7-bit digits on the
+    # GSW-bit branch of the expansion (about 1 decode in 240 fails); its runs
+    # use t_exp_right = 16 (4-bit digits), the first-dimension branch keeps 8.
+    p8 = dataclasses.replace(p, t_exp_right=16)
+    out = {"suite": True}
+    key_sets = [C.Client(p, seed=100 + k) for k in range(8)]
+    keys = [cl.public_keys(9, 11) for cl in key_sets]
+    key_sets8 = [C.Client(p8, seed=100 + k) for k in range(8)]
+    keys8 = [cl.public_keys(9, 11) for cl in key_sets8]
+    shapes = {"64MiB": P.SHAPE_64MIB, "1GiB": P.SHAPE_1GIB, "8GiB": P.SHAPE_8GIB}
+    recs = {}
+    t0 = time.perf_counter()
+    recs["64MiB"] = C.random_records(P.SHAPE_64MIB, p, seed=201)
+    recs["1GiB"] = C.random_records(P.SHAPE_1GIB, p, seed=202)
+    if not args.skip_8gib:
+        recs["8GiB"] = C.random_records(P.SHAPE_8GIB, p, seed=203)
+    gen_s = time.perf_counter() - t0
+    rng = np.random.default_rng(7)
+
+    def query_for(k, name, ks=None):
+        sh = shapes[name]
+        idx = int(rng.integers(0, sh.num_records))
+        return (ks or key_sets)[k].query(sh, idx), idx
+
+    # uneven batches: 1 GiB and 64 MiB queries mixed in one batch
+    g = SpiralGPU(p, max_batch=64)
+    for k in range(8):
+        g.set_client_keys(k, keys[k])
+    g.load_db(1, recs["1GiB"], 9, 8)
+    g.load_db(2, recs["64MiB"], 8, 5)
+    single = []
+    for name, db in (("1GiB", 1), ("64MiB", 2)):
+        q, idx = query_for(0, name)
+        g.answer(0, db, q)
+        t1 = time.perf_counter()
+        for _ in range(5):
+            r = g.answer(0, db, q)
+        single.append({"db": name, "e2e_ms": (time.perf_counter() - t1) / 5 * 1e3,
+                       "ok": bool(np.array_equal(key_sets[0].decode(r), recs[name][idx]))})
+    out["single"] = single
+    uneven = []
+    for B in (8, 32, 64):
+        reqs, checks = [], []
+        for s in range(B):
+            name, db = ("1GiB", 1) if s % 2 == 0 else ("64MiB", 2)
+            k = s % 8
+            q, idx = query_for(k, name)
+            reqs.append((k, db, q))
+            checks.append((k, name, idx))
+        # staged (device-resident) timing: slots must be in database order
+        order = sorted(range(B), key=lambda s: reqs[s][1])
+        for slot, s in enumerate(order):
+            g.stage_query(slot, reqs[s][0], reqs[s][1], reqs[s][2])
+        g.time_staged(B, 1)
+        ms = g.time_staged(B, 3)
+        g.stats_reset()
+        g.run_staged(B)
+        st = g.stats()
+        resp = g.answer_batch(reqs)
+        ok = all(np.array_equal(key_sets[k].decode(r), recs[name][idx]) for r, (k, name, idx) in zip(resp, checks))
+        uneven.append({"B": B, "mix": "1GiB:64MiB = 1:1", "ms_per_batch": ms, "queries_per_s": B / ms * 1e3,
+                       "stages_ms": {k[3:]: st[k] for k in ("ms_expand", "ms_convert", "ms_db_mul", "ms_fold",
+                                                           "ms_pack", "ms_total")},
+                       "decoded_ok": ok})
+    out["uneven_batches"] = uneven
+    print(json.dumps({"suite": "uneven_batches", "single": single, "uneven_batches": uneven}), flush=True)
+    g.close()
+
+    # 8 GiB database: 2^20 records, 64 GiB device image
+    if not args.skip_8gib:
+        g = SpiralGPU(p8, max_batch=16)
+        g.set_client_keys(0, keys8[0])
+        t1 = time.perf_counter()
+        g.load_db(3, recs["8GiB"], 9, 11)
+        load_s = time.perf_counter() - t1
+        q, idx = query_for(0, "8GiB", key_sets8)
+        r = g.answer(0, 3, q)
+        ok = bool(np.array_equal(key_sets8[0].decode(r), recs["8GiB"][idx]))
+        g.stage_query(0, 0, 3, q)
+        g.time_staged(1, 1)
+        ms1 = g.time_staged(1, 3)
+        mul = g.time_db_mul(3, 1, 3)
+        img = (1 << 20) * 4 * 2048 * 8
+        abytes = img + 512 * 2048 * 16 + 4 * 2048 * 4 * 2048 * 4
+        for s in range(16):
+            g.stage_query(s, 0, 3, q)
+        g.time_staged(16, 1)
+        ms16 = g.time_staged(16, 2)
+        ok16 = all(np.array_equal(key_sets8[0].decode(g.fetch_response(s)), recs["8GiB"][idx]) for s in range(16))
+        peak, _ = measured_peaks()
+        out["db_8gib"] = {"t_exp_right": 16, "load_s": load_s, "decoded_ok": ok, "single_ms": ms1, "single_qps": 1e3 / ms1,
+                          "db_mul_ms": mul, "db_mul_gbs": abytes / mul / 1e6, "db_mul_frac": abytes / mul / 1e6 / peak,
+                          "B16_ms": ms16, "B16_qps": 16e3 / ms16, "B16_decoded_ok": ok16}
+        print(json.dumps({"suite": "db_8gib", **out["db_8gib"]}), flush=True)
+        g.close()
+
+    # serving: three resident databases, 256 clients, HBM budget with LRU eviction
+    names = ["64MiB", "1GiB"] + ([] if args.skip_8gib else ["8GiB"])
+    ids = {n: i + 1 for i, n in enumerate(names)}
+    key_bytes = sum(a.nbytes for a in (keys8[0].exp_left, keys8[0].exp_right, keys8[0].conv, keys8[0].pack))
+
+    def serving_ctx(budget):
+        g = SpiralGPU(p8, max_batch=32, hbm_budget_bytes=budget)
+        for n in names:
+            g.load_db(ids[n], recs[n], shapes[n].nu1, shapes[n].nu2)
+        for k in range(8):
+            g.set_client_keys(k, keys8[k])
+        srv = Server(g, lanes=2)      # reserves both lanes' workspace
+        return g, srv
+
+    g, srv = serving_ctx(0)
+    used = g.hbm_used()
+    srv.stop()
+    g.close()
+    budget = used + 120 * key_bytes          # room for ~128 clients' keys; 256 share it by LRU
+    g, srv = serving_ctx(budget)
+    serving, registered = [], 0
+    for rate in (250.0, 500.0, 1000.0, 2000.0, 4000.0):
+        active = rng.choice(256, size=96, replace=False)
+        for cid in active:               # registering evicts the least recently used clients
+            g.set_client_keys(int(cid), keys8[int(cid) % 8])
+            registered += 1
+        n_req = int(min(600, max(200, rate * 0.5)))
+        reqs, checks = [], []
+        for _ in range(n_req):
+            cid = int(active[int(rng.integers(0, len(active)))])
+            name = names[int(rng.integers(0, len(names)))]
+            q, idx = query_for(cid % 8, name, key_sets8)
+            reqs.append((cid, ids[name], q))
+            checks.append((cid, name, idx))
+        res = poisson_load(srv, reqs, rate_qps=rate, seed=int(rate))
+        wrong = {}
+        for r, (cid, name, idx) in zip(res.pop("responses"), checks):
+            if not np.array_equal(key_sets8[cid % 8].decode(r), recs[name][idx]):
+                wrong[name] = wrong.get(name, 0) + 1
+        res["decoded_ok"] = not wrong
+        if wrong:
+            res["wrong_by_db"] = wrong
+        serving.append(res)
+    st = srv.stats()
+    srv.stop()
+    out["serving"] = {"t_exp_right": 16, "dbs": names, "clients": 256, "hbm_budget_bytes": budget, "key_bytes_per_client": key_bytes,
+                      "client_registrations": registered, "lanes": 2, "max_batch": 32, "rates": serving,
+                      "batches": st["batches"], "served": st["served"]}
+    g.close()
+    print(json.dumps({"suite": "serving", **out["serving"], "record_gen_s": gen_s}), flush=True)
 
 
 if __name__ == "__main__":

@@ -78,6 +78,17 @@ __device__ __forceinline__ uint32_t to_mont(uint32_t x, const Prime &c) {  // ca
     return min(y, y - c.p);
 }
 
+int sm_count() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 148;
+    }
+    return n;
+}
+
 }  // namespace
 
 // ------------------------------------------------------------ conversions
@@ -127,9 +138,12 @@ cudaError_t launch_widen(const uint32_t *in, uint64_t *out, uint64_t planes, boo
 // and x^(-2^r) * v[i - 2^r] above; the output is
 //   v + [0; tau(v).row1] + W_r * NTT(G^-1(raw(tau(v).row0)))
 // with tau = x -> x^(D/2^r + 1) applied as a slot permutation in NTT form.
-__global__ void __launch_bounds__(THREADS) k_expand_round(const QDesc *__restrict__ qd, int r, StageParams sp,
-                                                         const TwiddleSet *__restrict__ tws,
-                                                         const uint32_t *__restrict__ neg1) {
+// GP groups per prime split the t_exp digit transforms (GP = 2 for rounds
+// with few outputs); with GP = 2 group (g, sub) finishes output row `sub`.
+template <int GP>
+__global__ void __launch_bounds__(256 * GP, 3 - GP) k_expand_round(const QDesc *__restrict__ qd, int r, StageParams sp,
+                                                          const TwiddleSet *__restrict__ tws,
+                                                          const uint32_t *__restrict__ neg1) {
     const QDesc &Q = qd[blockIdx.y];
     const int i = blockIdx.x;
     if (!Q.active || r >= Q.g || i >= (2 << r)) return;
@@ -137,28 +151,44 @@ __global__ void __launch_bounds__(THREADS) k_expand_round(const QDesc *__restric
     if (Q.stop > 0 && r > Q.stop && (i & 1)) return;
     if (Q.stop > 0 && r == Q.stop && (i & 1) && (i / 2) >= max_bits) return;
     extern __shared__ __align__(16) uint32_t smem[];
-    const Ctx x = setup(smem, tws);
-    const Prime &c = x.c;
+    load_twiddles(smem, tws);
+    const int gi = threadIdx.x >> 7, g = gi & 1, sub = gi >> 1, t = threadIdx.x & (GROUP - 1), bar = 1 + gi;
+    const Prime c = prime_of(g);
+    uint32_t *bufs = smem + 4 * D;
+    uint32_t *buf = bufs + gi * 2 * D;
+    const uint32_t *twf = smem + g * D, *twi = smem + (2 + g) * D;
+    __syncthreads();
     const int half = 1 << r;
     const bool upper = i >= half;
     const uint32_t *ct = r == 0 ? Q.query : Q.v[r & 1] + (size_t)(upper ? i - half : i) * 4 * D;
-    const uint32_t *n1 = neg1 + ((size_t)r * 2 + x.g) * D;
+    const uint32_t *n1 = neg1 + ((size_t)r * 2 + g) * D;
     const uint32_t tau = (uint32_t)(D >> r) + 1;
-    const uint32_t *row0 = ct + x.g * D, *row1 = ct + (2 + x.g) * D;
 
-    // tau(row0) in NTT form -> raw
-    uint64_t raw[VPT];
-    {
+    // raw(tau(row0)): INTT by the sub-0 group of each prime, inverse CRT by all
+    if (sub == 0) {
+        const uint32_t *row0 = ct + g * D;
         uint32_t v[VPT];
 #pragma unroll
         for (int j = 0; j < VPT; j++) {
-            const int zs = auto_slot(VPT * x.t + j, tau);
-            uint32_t a = row0[zs];
+            const int zs = auto_slot(VPT * t + j, tau);
+            const uint32_t a = row0[zs];
             v[j] = upper ? mont_mul(a, n1[zs], c.p, c.pinv) : a;   // (0, 2p)
         }
-        ntt_inv(v, tw_inv(x), x.buf, c, x.t, x.bar);
-        exchange_icrt(x, v, raw);
+        ntt_inv(v, twi, buf, c, t, bar);
+#pragma unroll
+        for (int j = 0; j < VPT; j++) buf[t + GROUP * j] = v[j];   // first buffer free since the INTT's 2nd barrier
     }
+    __syncthreads();
+    // raw coefficients in shared memory (after the groups' buffers); each
+    // group writes 16/(2*GP) of every thread's positions
+    uint64_t *raws = reinterpret_cast<uint64_t *>(bufs + 2 * GP * 2 * D);
+#pragma unroll
+    for (int j = 0; j < VPT; j++) {
+        if ((j * 2 * GP) / VPT != gi) continue;
+        const int e = t + GROUP * j;
+        raws[e] = icrt(bufs[e], bufs[2 * D + e]);
+    }
+    __syncthreads();
     const bool left = (r != 0) && !(i & 1);
     const int tk = left ? sp.t_left : sp.t_right;
     const uint32_t *W = (left ? Q.left : Q.right) + (size_t)r * 2 * tk * 2 * D;
@@ -167,60 +197,76 @@ __global__ void __launch_bounds__(THREADS) k_expand_round(const QDesc *__restric
     uint32_t acc0[VPT], acc1[VPT];
 #pragma unroll
     for (int j = 0; j < VPT; j++) acc0[j] = acc1[j] = 0;
-    for (int k = 0; k < tk; k++) {
+#pragma unroll 1
+    for (int k = sub; k < tk; k += GP) {
         uint32_t d[VPT];
-        digits(d, raw, bits * k, mask);
-        ntt_fwd(d, tw_fwd(x), x.buf, c, x.t, x.bar);
-        mac16(acc0, d, W + ((size_t)(0 * tk + k) * 2 + x.g) * D + VPT * x.t, c);
-        mac16(acc1, d, W + ((size_t)(1 * tk + k) * 2 + x.g) * D + VPT * x.t, c);
+#pragma unroll
+        for (int j = 0; j < VPT; j++) d[j] = (uint32_t)((raws[t + GROUP * j] >> (bits * k)) & mask);
+        ntt_fwd(d, twf, buf, c, t, bar);
+        mac16(acc0, d, W + ((size_t)(0 * tk + k) * 2 + g) * D + VPT * t, c);
+        mac16(acc1, d, W + ((size_t)(1 * tk + k) * 2 + g) * D + VPT * t, c);
     }
-    // v + acc (+ tau(row1) on row 1)
-    uint32_t o0[VPT], o1[VPT];
-    {
-        uint32_t b0[VPT], b1[VPT];
-        ld16(b0, row0 + VPT * x.t);
-        ld16(b1, row1 + VPT * x.t);
-        uint32_t nn[VPT];
-        if (upper) ld16(nn, n1 + VPT * x.t);
+    if constexpr (GP == 2) {
+        group_sync(bar);
+        if (sub == 0) st16(buf + VPT * t, acc1); else st16(buf + VPT * t, acc0);
+        __syncthreads();
+        uint32_t w[VPT];
+        ld16(w, bufs + (g + 2 * (1 - sub)) * 2 * D + VPT * t);
 #pragma unroll
         for (int j = 0; j < VPT; j++) {
-            const int zs = auto_slot(VPT * x.t + j, tau);
-            uint32_t tb = row1[zs];
-            if (upper) {
-                tb = reduce2(mont_mul(tb, n1[zs], c.p, c.pinv), c.p);
-                b0[j] = reduce2(mont_mul(b0[j], nn[j], c.p, c.pinv), c.p);
-                b1[j] = reduce2(mont_mul(b1[j], nn[j], c.p, c.pinv), c.p);
-            }
-            o0[j] = canon4(b0[j] + acc0[j], c.p);
-            o1[j] = canon4(canon4(b1[j] + acc1[j], c.p) + tb, c.p);
+            if (sub == 0) acc0[j] = reduce2(acc0[j] + w[j], 2 * c.p);
+            else acc1[j] = reduce2(acc1[j] + w[j], 2 * c.p);
         }
     }
-    const int zb = VPT * x.t;
-    if (r + 1 < Q.g) {
-        uint32_t *out = Q.v[(r + 1) & 1] + (size_t)i * 4 * D;
-        st16(out + x.g * D + zb, o0);
-        st16(out + (2 + x.g) * D + zb, o1);
-    }
-    if (r == Q.capture && (i & 1) && (i / 2) < max_bits) {
-        uint32_t *out = Q.gsw_in + (size_t)(i / 2) * 4 * D;
-        st16(out + x.g * D + zb, o0);
-        st16(out + (2 + x.g) * D + zb, o1);
-    }
-    if (r == Q.g - 1 && !(i & 1) && (i / 2) < (1 << Q.nu1)) {
-        uint32_t *s = Q.sel + (size_t)(i / 2) * D * 4;
+    // output rows: row 0 = v.row0 + acc0, row 1 = v.row1 + acc1 + tau(v.row1)
+    const int zb = VPT * t;
+    const int first = GP == 2 ? sub : 0, last = GP == 2 ? sub : 1;
+    for (int row = first; row <= last; row++) {
+        const uint32_t *src = ct + (row * 2 + g) * D;
+        uint32_t o[VPT];
+        ld16(o, src + zb);
+        if (upper) {
+            uint32_t nn[VPT];
+            ld16(nn, n1 + zb);
 #pragma unroll
-        for (int j = 0; j < VPT; j++) {
-            s[(zb + j) * 4 + x.g] = o0[j];
-            s[(zb + j) * 4 + 2 + x.g] = o1[j];
+            for (int j = 0; j < VPT; j++) o[j] = reduce2(mont_mul(o[j], nn[j], c.p, c.pinv), c.p);
+        }
+#pragma unroll
+        for (int j = 0; j < VPT; j++) o[j] = canon4(o[j] + (row == 0 ? acc0[j] : acc1[j]), c.p);
+        if (row == 1) {
+#pragma unroll
+            for (int j = 0; j < VPT; j++) {
+                const int zs = auto_slot(zb + j, tau);
+                uint32_t tb = src[zs];
+                if (upper) tb = reduce2(mont_mul(tb, n1[zs], c.p, c.pinv), c.p);
+                o[j] = canon4(o[j] + tb, c.p);
+            }
+        }
+        if (r + 1 < Q.g) st16(Q.v[(r + 1) & 1] + (size_t)i * 4 * D + (row * 2 + g) * D + zb, o);
+        if (r == Q.capture && (i & 1) && (i / 2) < max_bits)
+            st16(Q.gsw_in + (size_t)(i / 2) * 4 * D + (row * 2 + g) * D + zb, o);
+        if (r == Q.g - 1 && !(i & 1) && (i / 2) < (1 << Q.nu1)) {
+            uint32_t *sl = Q.sel + (size_t)(i / 2) * D * 4;
+#pragma unroll
+            for (int j = 0; j < VPT; j++) sl[(zb + j) * 4 + row * 2 + g] = o[j];
         }
     }
 }
 
 cudaError_t launch_expand_round(const QDesc *qd, int nq, int r, int max_out, const StageParams &sp,
                                 const TwiddleSet *tw, const uint32_t *neg1, cudaStream_t st) {
-    cudaError_t e = cudaFuncSetAttribute(k_expand_round, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-    if (e != cudaSuccess) return e;
-    k_expand_round<<<dim3(max_out, nq), THREADS, SMEM_BYTES, st>>>(qd, r, sp, tw, neg1);
+    const bool wide = (uint64_t)max_out * nq < 2ull * sm_count();
+    if (wide) {
+        const int smem = (4 * D + 4 * 2 * D) * 4 + D * 8;
+        cudaError_t e = cudaFuncSetAttribute(k_expand_round<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        k_expand_round<2><<<dim3(max_out, nq), 512, smem, st>>>(qd, r, sp, tw, neg1);
+    } else {
+        const int smem = SMEM_BYTES + D * 8;
+        cudaError_t e = cudaFuncSetAttribute(k_expand_round<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        k_expand_round<1><<<dim3(max_out, nq), THREADS, smem, st>>>(qd, r, sp, tw, neg1);
+    }
     return cudaGetLastError();
 }
 
@@ -274,7 +320,7 @@ cudaError_t launch_sel_import(const uint64_t *in, uint32_t *sel, int rows, cudaS
 // Item blockIdx.x = dim*t_gsw + j: GSW column 2j+1 = the Regev encoding,
 // column 2j = V * NTT(G^-1_{2,t_conv}(raw(c))).  Output in Montgomery form
 // (the fold multiplies by it).
-__global__ void __launch_bounds__(THREADS) k_regev_to_gsw(const QDesc *__restrict__ qd, StageParams sp,
+__global__ void __launch_bounds__(THREADS, 2) k_regev_to_gsw(const QDesc *__restrict__ qd, StageParams sp,
                                                          const TwiddleSet *__restrict__ tws) {
     const QDesc &Q = qd[blockIdx.y];
     const int idx = blockIdx.x;
@@ -292,6 +338,7 @@ __global__ void __launch_bounds__(THREADS) k_regev_to_gsw(const QDesc *__restric
     uint32_t acc0[VPT], acc1[VPT];
 #pragma unroll
     for (int j = 0; j < VPT; j++) acc0[j] = acc1[j] = 0;
+#pragma unroll 1
     for (int row = 0; row < 2; row++) {
         uint64_t raw[VPT];
         {
@@ -300,6 +347,7 @@ __global__ void __launch_bounds__(THREADS) k_regev_to_gsw(const QDesc *__restric
             ntt_inv(v, tw_inv(x), x.buf, c, x.t, x.bar);
             exchange_icrt(x, v, raw);
         }
+#pragma unroll 1
         for (int k = 0; k < sp.t_conv; k++) {
             uint32_t d[VPT];
             digits(d, raw, bits * k, mask);
@@ -364,16 +412,27 @@ cudaError_t launch_gsw_neg(const uint32_t *gsw, uint32_t *neg, int count, int t,
 // which equals C*G^-1(v[num_per+i]) + (G - C)*G^-1(v[i]) exactly
 // (G*G^-1(x) = x for the unsigned digits), the fold of
 // gpu-pir/folding.cuh:9-27 with one product instead of two.
-__global__ void __launch_bounds__(THREADS) k_fold_level(const QDesc *__restrict__ qd, int level, StageParams sp,
-                                                       const TwiddleSet *__restrict__ tws) {
+//
+// GP groups of 128 threads per prime share one fold: the 2*t_gsw digit
+// transforms are split between them, partial products are added through
+// shared memory, and with GP = 2 each group finishes one output row.
+// GP = 2 halves the latency of a fold and is used when a level has few folds.
+template <int GP>
+__global__ void __launch_bounds__(256 * GP, 3 - GP) k_fold_level(const QDesc *__restrict__ qd, int level, StageParams sp,
+                                                        const TwiddleSet *__restrict__ tws) {
     const QDesc &Q = qd[blockIdx.y];
     if (!Q.active || level >= Q.nu2) return;
     const int num_per = 1 << (Q.nu2 - 1 - level);
     const int inst = blockIdx.x / num_per, i = blockIdx.x % num_per;
     if (inst >= sp.T) return;
     extern __shared__ __align__(16) uint32_t smem[];
-    const Ctx x = setup(smem, tws);
-    const Prime &c = x.c;
+    load_twiddles(smem, tws);
+    const int gi = threadIdx.x >> 7, g = gi & 1, sub = gi >> 1, t = threadIdx.x & (GROUP - 1), bar = 1 + gi;
+    const Prime c = prime_of(g);
+    uint32_t *bufs = smem + 4 * D;           // [group][2][D]
+    uint32_t *buf = bufs + gi * 2 * D;
+    const uint32_t *twf = smem + g * D, *twi = smem + (2 + g) * D;
+    __syncthreads();
     const int cols = 1 << Q.nu2;
     uint64_t *base = Q.raw + (size_t)inst * cols * 2 * D;
     uint64_t *v0 = base + (size_t)i * 2 * D;
@@ -385,49 +444,83 @@ __global__ void __launch_bounds__(THREADS) k_fold_level(const QDesc *__restrict_
     uint32_t acc0[VPT], acc1[VPT];
 #pragma unroll
     for (int j = 0; j < VPT; j++) acc0[j] = acc1[j] = 0;
-    for (int row = 0; row < 2; row++) {
-        for (int k = 0; k < tg; k++) {
-            const int sh = bits * k;
-            uint32_t d[VPT];
+#pragma unroll 1
+    for (int pr = sub; pr < 2 * tg; pr += GP) {
+        const int row = pr / tg, k = pr % tg;
+        const int sh = bits * k;
+        uint32_t d[VPT];
 #pragma unroll
-            for (int j = 0; j < VPT; j++) {
-                const int e = x.t + GROUP * j;
-                const uint32_t a = (uint32_t)((__ldg(v1 + row * D + e) >> sh) & mask);
-                const uint32_t b = (uint32_t)((v0[row * D + e] >> sh) & mask);
-                d[j] = a >= b ? a - b : a + c.p - b;
-            }
-            ntt_fwd(d, tw_fwd(x), x.buf, c, x.t, x.bar);
-            const int col = row + 2 * k;
-            mac16(acc0, d, C + ((size_t)(0 * gc + col) * 2 + x.g) * D + VPT * x.t, c);
-            mac16(acc1, d, C + ((size_t)(1 * gc + col) * 2 + x.g) * D + VPT * x.t, c);
+        for (int j = 0; j < VPT; j++) {
+            const int e = t + GROUP * j;
+            const uint32_t a = (uint32_t)((__ldg(v1 + row * D + e) >> sh) & mask);
+            const uint32_t b = (uint32_t)((v0[row * D + e] >> sh) & mask);
+            d[j] = a >= b ? a - b : a + c.p - b;
         }
+        ntt_fwd(d, twf, buf, c, t, bar);
+        const int col = row + 2 * k;
+        mac16(acc0, d, C + ((size_t)(0 * gc + col) * 2 + g) * D + VPT * t, c);
+        mac16(acc1, d, C + ((size_t)(1 * gc + col) * 2 + g) * D + VPT * t, c);
     }
-    ntt_inv(acc0, tw_inv(x), x.buf, c, x.t, x.bar);
-    ntt_inv(acc1, tw_inv(x), x.buf, c, x.t, x.bar);
-    group_sync(x.bar);  // this group's last transpose reads are done
-    uint32_t *ex0 = x.bufs + x.g * 2 * D, *ex1 = ex0 + D;   // [row][prime] = bufs + (prime*2 + row)*D
+    if constexpr (GP == 1) {
+        ntt_inv(acc0, twi, buf, c, t, bar);
+        ntt_inv(acc1, twi, buf, c, t, bar);
+        group_sync(bar);  // this group's last transpose reads are done
+        uint32_t *ex0 = buf, *ex1 = buf + D;   // [prime][row] = bufs + (prime*2 + row)*D
 #pragma unroll
-    for (int j = 0; j < VPT; j++) {
-        ex0[x.t + GROUP * j] = acc0[j];
-        ex1[x.t + GROUP * j] = acc1[j];
-    }
-    __syncthreads();
-    // group g finishes row g
-    const int row = x.g;
-    const uint32_t *a0 = x.bufs + row * D, *a1 = x.bufs + 2 * D + row * D;
+        for (int j = 0; j < VPT; j++) {
+            ex0[t + GROUP * j] = acc0[j];
+            ex1[t + GROUP * j] = acc1[j];
+        }
+        __syncthreads();
+        const int row = g;   // group g finishes row g
+        const uint32_t *a0 = bufs + row * D, *a1 = bufs + 2 * D + row * D;
 #pragma unroll
-    for (int j = 0; j < VPT; j++) {
-        const int e = x.t + GROUP * j;
-        uint64_t y = icrt(a0[e], a1[e]) + v0[row * D + e];
-        v0[row * D + e] = y >= QQ ? y - QQ : y;
+        for (int j = 0; j < VPT; j++) {
+            const int e = t + GROUP * j;
+            uint64_t y = icrt(a0[e], a1[e]) + v0[row * D + e];
+            v0[row * D + e] = y >= QQ ? y - QQ : y;
+        }
+    } else {
+        // group (g, sub) finishes row `sub`: hand the other row to the partner
+        group_sync(bar);
+        if (sub == 0) st16(buf + VPT * t, acc1); else st16(buf + VPT * t, acc0);
+        __syncthreads();
+        uint32_t w[VPT];
+        ld16(w, bufs + (g + 2 * (1 - sub)) * 2 * D + VPT * t);
+        uint32_t a[VPT];
+#pragma unroll
+        for (int j = 0; j < VPT; j++) a[j] = reduce2((sub == 0 ? acc0[j] : acc1[j]) + w[j], 2 * c.p);
+        __syncthreads();   // partner has read this group's buffer
+        ntt_inv(a, twi, buf, c, t, bar);
+        group_sync(bar);
+#pragma unroll
+        for (int j = 0; j < VPT; j++) buf[t + GROUP * j] = a[j];
+        __syncthreads();
+        const int row = sub;
+        const uint32_t *a0 = bufs + (2 * row) * 2 * D, *a1 = bufs + (1 + 2 * row) * 2 * D;
+#pragma unroll
+        for (int j = 0; j < VPT; j++) {
+            if ((j >> 3) != g) continue;     // the two primes' groups split the positions
+            const int e = t + GROUP * j;
+            uint64_t y = icrt(a0[e], a1[e]) + v0[row * D + e];
+            v0[row * D + e] = y >= QQ ? y - QQ : y;
+        }
     }
 }
 
 cudaError_t launch_fold_level(const QDesc *qd, int nq, int level, int max_items, const StageParams &sp,
                               const TwiddleSet *tw, cudaStream_t st) {
-    cudaError_t e = cudaFuncSetAttribute(k_fold_level, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-    if (e != cudaSuccess) return e;
-    k_fold_level<<<dim3(max_items, nq), THREADS, SMEM_BYTES, st>>>(qd, level, sp, tw);
+    const bool wide = (uint64_t)max_items * nq < 2ull * sm_count();
+    if (wide) {
+        const int smem = (4 * D + 4 * 2 * D) * 4;
+        cudaError_t e = cudaFuncSetAttribute(k_fold_level<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        k_fold_level<2><<<dim3(max_items, nq), 512, smem, st>>>(qd, level, sp, tw);
+    } else {
+        cudaError_t e = cudaFuncSetAttribute(k_fold_level<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        if (e != cudaSuccess) return e;
+        k_fold_level<1><<<dim3(max_items, nq), THREADS, SMEM_BYTES, st>>>(qd, level, sp, tw);
+    }
     return cudaGetLastError();
 }
 
@@ -447,7 +540,7 @@ constexpr int PACK_MAX_N = 2;
 // Column c = blockIdx.x of query blockIdx.y: sum over r < n of
 // W_r * NTT(G^-1(ct[r*n+c].row0)) + e_{1+r} * NTT(ct[r*n+c].row1), then raw,
 // then row 0 rescaled to 2^q2_bits and rows 1..n to 4p.
-__global__ void __launch_bounds__(THREADS) k_pack(const QDesc *__restrict__ qd, StageParams sp,
+__global__ void __launch_bounds__(THREADS, 2) k_pack(const QDesc *__restrict__ qd, StageParams sp,
                                                  const TwiddleSet *__restrict__ tws) {
     const QDesc &Q = qd[blockIdx.y];
     const int col = blockIdx.x;
@@ -470,6 +563,7 @@ __global__ void __launch_bounds__(THREADS) k_pack(const QDesc *__restrict__ qd, 
         uint64_t raw[VPT];
 #pragma unroll
         for (int j = 0; j < VPT; j++) raw[j] = ct[x.t + GROUP * j];
+#pragma unroll 1
         for (int k = 0; k < tcv; k++) {
             uint32_t d[VPT];
             digits(d, raw, bits * k, mask);

@@ -572,6 +572,11 @@ static int db_check_shape(sp_ctx *c, int nu1, int nu2) {
     if (nu1 < 1 || nu1 > 14 || nu2 < 1 || nu2 > 14) return fail(SP_ERR_INVALID, "nu1/nu2 out of range");
     if (shape_of(c, nu1, nu2).g > LOGD)
         return fail(SP_ERR_UNSUPPORTED, "expansion needs more than 11 rounds (t_gsw*nu2 + 2^nu1 > 2048)");
+    // the expansion interleaves 2^nu1 selectors (even outputs) with t_gsw*nu2
+    // GSW-bit encodings (odd outputs) in 2^g outputs: both halves must fit
+    if (((uint64_t)c->sp.t_gsw * nu2 << 1) > (1ull << shape_of(c, nu1, nu2).g))
+        return fail(SP_ERR_UNSUPPORTED, "t_gsw*nu2 GSW-bit encodings do not fit the odd expansion outputs "
+                                        "(needs 2^nu1 >= t_gsw*nu2)");
     DbLayout L = make_db_layout(c->sp.T, nu1, nu2);
     const int tcg = L.T * L.cg;
     if (tcg != 4 && tcg != 8 && tcg != 16)
@@ -1321,9 +1326,20 @@ int sp_serve_start(sp_ctx *c, int32_t lanes) {
     if (lanes < 1 || lanes > 8) return fail(SP_ERR_INVALID, "lanes must be in [1, 8]");
     std::lock_guard<std::mutex> lk(c->mu);
     if (c->serving) return fail(SP_ERR_INVALID, "already serving");
+    // every lane reserves max_batch workspace slots for the largest loaded
+    // database shape now, so admission later only depends on the HBM budget
+    // left for client keys
+    Shape need{};
+    for (auto &kv : c->dbs) {
+        Shape s = shape_of(c, kv.second.L.nu1, kv.second.L.nu2);
+        need.nu1 = std::max(need.nu1, s.nu1);
+        need.nu2 = std::max(need.nu2, s.nu2);
+        need.g = std::max(need.g, s.g);
+    }
     for (int i = 0; i < lanes; i++) {
         Lane *L = new Lane();
         int rc = lane_init(c, *L, c->p.max_batch);
+        if (!rc && need.g) rc = ensure_slots(c, *L, need, c->p.max_batch);
         c->lanes.push_back(L);
         if (rc) {
             for (Lane *x : c->lanes) {

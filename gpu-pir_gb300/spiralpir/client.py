@@ -143,6 +143,8 @@ class Client:
         if not (0 <= row < shape.rows):
             raise IndexError("record index out of range")
         g = p.g(shape.nu1, shape.nu2)
+        if 2 * p.t_gsw * shape.nu2 > (1 << g):
+            raise ValueError("2^nu1 must be at least t_gsw*nu2 for the expansion layout")
         rest = min(p.stop_round(shape.nu2) + 1, g)
         sigma = np.zeros(D, dtype=object)
         sigma[2 * row] = delta(p) * pow(1 << g, -1, Q) % Q
@@ -178,6 +180,31 @@ class Client:
                 v = (ring.rescale_small(prod, q2, q1) + rest[r, c]) % q1
                 out[r * n + c] = ring.rescale_small(v, q1, p.p).astype(np.uint8)
         return out
+
+    def decode_margin(self, response: np.ndarray, expected: np.ndarray) -> float:
+        """Largest distance, in units of the rows' modulus 4p, between the
+        value decoded before the final rounding and its expected plaintext
+        multiple (decoding fails at 2.0)."""
+        p = self.params
+        n, q2, q1 = p.n, 1 << p.q2_bits, 1 << (p.pt_bits + 2)
+        bits = np.unpackbits(np.asarray(response, dtype=np.uint8), bitorder="little")
+        first_cnt, rest_cnt = n * D, n * n * D
+        b0 = bits[: first_cnt * p.q2_bits].reshape(first_cnt, p.q2_bits).astype(np.int64)
+        first = (b0 << np.arange(p.q2_bits, dtype=np.int64)).sum(axis=1).reshape(n, D)
+        q1b = p.pt_bits + 2
+        off = first_cnt * p.q2_bits
+        b1 = bits[off: off + rest_cnt * q1b].reshape(rest_cnt, q1b).astype(np.int64)
+        rest = (b1 << np.arange(q1b, dtype=np.int64)).sum(axis=1).reshape(n, n, D)
+        worst = 0.0
+        for r in range(n):
+            for c in range(n):
+                prod = ring.negacyclic_mul_small(self.s_gsw[r], first[c], q2)
+                exact = prod.astype(np.float64) * q1 / q2            # unrounded rescale
+                v = (exact + rest[r, c]) % q1
+                m = expected[r * n + c].astype(np.float64) * (q1 // p.p)
+                d = np.abs(((v - m + q1 / 2) % q1) - q1 / 2)
+                worst = max(worst, float(d.max()))
+        return worst
 
     def decode_noise(self, packed_raw: np.ndarray, expected: np.ndarray) -> float:
         """log2 of the largest |noise| of a packed (n+1) x n raw ciphertext

@@ -147,7 +147,9 @@ int sp_set_db_mul_variant(sp_ctx *ctx, int32_t variant);
  * on the GPU.  The response is written to the request's buffer before the
  * ticket completes (sp_poll / sp_wait); a request that cannot run (unknown
  * ids, keys that do not cover the database, workspace beyond the HBM
- * budget) completes with its error status.  sp_serve_stop drains the queue. */
+ * budget) completes with its error status.  sp_serve_start reserves each
+ * lane's workspace for the largest database loaded at that time.
+ * sp_serve_stop drains the queue. */
 int sp_serve_start(sp_ctx *ctx, int32_t lanes);
 int sp_serve_stop(sp_ctx *ctx);
 int sp_submit(sp_ctx *ctx, const sp_request *req, uint64_t *ticket);

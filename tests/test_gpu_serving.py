@@ -90,3 +90,57 @@ def test_serving_poisson_and_errors(world):
     for x, y in zip(res["responses"], alone):
         assert np.array_equal(x, y)
     assert res["p99_ms"] >= res["p50_ms"] > 0
+
+
+@pytest.mark.parametrize("variant", [1, 2])
+def test_batch_many_columns(variant):
+    """nu2 = 10 (1024 columns, 256 column groups): batched multiply grid and
+    10 fold levels; each result decodes and equals the query answered alone."""
+    p = P.PARAMS
+    sh = P.DbShape(7, 10)
+    recs = C.random_records(sh, p, seed=91)
+    cl = C.Client(p, seed=92)
+    with SpiralGPU(p, max_batch=6) as gpu:
+        gpu.set_client_keys(1, cl.public_keys(7, 10))
+        gpu.load_db(1, recs, sh.nu1, sh.nu2)
+        idx = [0, 77, 5000, sh.num_records - 1, 123456, 9]
+        qs = [cl.query(sh, i) for i in idx]
+        alone = [gpu.answer(1, 1, q) for q in qs]
+        for i, r in zip(idx, alone):
+            assert np.array_equal(cl.decode(r), recs[i])
+        gpu.set_db_mul_variant(variant)
+        batch = gpu.answer_batch([(1, 1, q) for q in qs])
+        for x, y in zip(batch, alone):
+            assert np.array_equal(x, y)
+
+
+def test_serving_mixed_shapes_two_lanes():
+    p = P.PARAMS
+    shapes = [P.DbShape(7, 10), P.SHAPE_8MIB, P.DbShape(6, 4)]
+    recs = [C.random_records(s, p, seed=93 + k) for k, s in enumerate(shapes)]
+    cl = C.Client(p, seed=96)
+    with SpiralGPU(p, max_batch=8) as gpu:
+        gpu.set_client_keys(1, cl.public_keys(7, 10))
+        for k, (s, r) in enumerate(zip(shapes, recs)):
+            gpu.load_db(k, r, s.nu1, s.nu2)
+        rng = np.random.default_rng(97)
+        reqs, checks = [], []
+        for _ in range(48):
+            k = int(rng.integers(0, 3))
+            i = int(rng.integers(0, shapes[k].num_records))
+            reqs.append((1, k, cl.query(shapes[k], i)))
+            checks.append((k, i))
+        with Server(gpu, lanes=2) as srv:
+            res = poisson_load(srv, reqs, rate_qps=20000.0, seed=4)
+        bad = [n for n, (r, (k, i)) in enumerate(zip(res["responses"], checks))
+               if not np.array_equal(cl.decode(r), recs[k][i])]
+        assert not bad, f"{len(bad)} of {len(reqs)} responses wrong: {[(n, checks[n]) for n in bad[:10]]}"
+
+
+def test_invalid_shape_rejected():
+    """2^nu1 < t_gsw*nu2: the GSW-bit encodings would not fit the odd
+    expansion outputs; the library refuses the database."""
+    with SpiralGPU(P.PARAMS) as gpu:
+        with pytest.raises(SpiralError) as e:
+            gpu.load_db(1, np.zeros((1 << 14, 4, 2048), np.uint8), 3, 11)
+        assert e.value.code == 6
