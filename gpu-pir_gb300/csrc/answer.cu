@@ -78,6 +78,9 @@ __device__ __forceinline__ uint32_t to_mont(uint32_t x, const Prime &c) {  // ca
     return min(y, y - c.p);
 }
 
+
+}  // namespace
+
 int sm_count() {
     static int n = 0;
     if (!n) {
@@ -88,8 +91,6 @@ int sm_count() {
     }
     return n;
 }
-
-}  // namespace
 
 // ------------------------------------------------------------ conversions
 __global__ void k_narrow(const uint64_t *__restrict__ in, uint32_t *__restrict__ out, uint64_t total, int to_m) {

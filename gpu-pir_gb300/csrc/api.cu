@@ -51,7 +51,7 @@ int ceil_log2(uint64_t x) {
 
 struct Db {
     DbLayout L{};
-    uint64_t *d = nullptr;
+    uint32_t *d = nullptr;
     uint64_t bytes = 0;
 };
 
@@ -95,6 +95,8 @@ struct Lane {
     cudaEvent_t ev[6]{};
     cudaEvent_t done = nullptr;
     int *d_err = nullptr;
+    uint8_t *limbs = nullptr;           // selector digit tiles of the tensor-core multiply
+    uint64_t limb_bytes = 0;
     int cap = 0;
     int staged = 0;
     bool busy = false;                  // serving: a batch is in flight
@@ -135,9 +137,10 @@ struct sp_ctx {
     std::mutex mu;
     sp_stats_out stats{};
     // multiply variant chosen per (database id, queries in the launch):
-    // 1 = per-query streaming kernel, 2 = batched kernel
+    // 1 = per-query streaming kernel, 2 = batched integer kernel,
+    // 3 = tensor-core kernel
     std::map<std::pair<int, int>, int> mul_choice;
-    int mul_force = 0;          // 0 = autotune, 1/2 = force a variant
+    int mul_force = 0;          // 0 = autotune, 1..3 = force a variant
     // serving (continuous batching)
     std::vector<Lane *> lanes;
     std::thread worker;
@@ -291,6 +294,9 @@ void lane_free(sp_ctx *c, Lane &L) {
     L.slots.clear();
     release(c, L.d_err, 16);
     release(c, L.d_qd, sizeof(QDesc) * L.cap);
+    release(c, L.limbs, L.limb_bytes);
+    L.limbs = nullptr;
+    L.limb_bytes = 0;
     L.d_err = nullptr;
     L.d_qd = nullptr;
     if (L.h_qd) cudaFreeHost(L.h_qd);
@@ -338,40 +344,90 @@ int check_client_for(const sp_ctx *c, const Client &cl, const Db &db, int *need_
     return SP_OK;
 }
 
+// Workspace of the tensor-core multiply for database layout `dl` (allocated
+// once per lane, under the HBM budget).  Returns false when it does not fit.
+bool ensure_limbs(sp_ctx *c, Lane &L, const DbLayout &dl) {
+    const uint64_t need = tc_limb_bytes(dl);
+    if (L.limb_bytes >= need) return true;
+    if (L.limbs) {
+        if (cudaStreamSynchronize(L.st) != cudaSuccess) return false;
+        release(c, L.limbs, L.limb_bytes);
+        L.limbs = nullptr;
+        L.limb_bytes = 0;
+    }
+    if (alloc(c, (void **)&L.limbs, need) != SP_OK) {
+        g_err.clear();
+        return false;
+    }
+    L.limb_bytes = need;
+    return true;
+}
+
+bool variant_available(sp_ctx *c, Lane &L, const Db &db, int nq, int variant) {
+    switch (variant) {
+        case 1: return true;
+        case 2: return nq >= 2 && db_mul_batch_supported(db.L);
+        case 3: return nq >= 2 && db_mul_tc_supported(db.L) && ensure_limbs(c, L, db.L);
+        default: return false;
+    }
+}
+
+// Enqueue the multiply of `nq` queries (descriptors qd) against `db`.
+cudaError_t launch_mul_variant(Lane &L, const Db &db, const QDesc *qd, int nq, int variant) {
+    switch (variant) {
+        case 2: return launch_db_mul_batch(db.d, db.L, qd, nq, L.st);
+        case 3:
+            for (int i = 0; i < nq; i += TC_MAX_Q) {
+                const int k = std::min(TC_MAX_Q, nq - i);
+                cudaError_t e = launch_db_mul_tc(db.d, db.L, qd + i, k, L.limbs, L.d_err, L.st);
+                if (e != cudaSuccess) return e;
+            }
+            return cudaSuccess;
+        default: return launch_db_mul(db.d, db.L, qd, nq, L.d_err, L.st);
+    }
+}
+
 // Autotuner of the first-dimension multiply: the first time a database is
-// multiplied for `nq` queries in one launch, both variants run once on the
-// (already staged) selectors and the faster, by CUDA events, is kept.
-// Their outputs are identical; the timed runs are overwritten by the real one.
+// multiplied for `nq` queries in one launch, every available variant runs
+// once on the (already staged) selectors and the fastest, by CUDA events, is
+// kept.  Their outputs are identical; the timed runs are overwritten by the
+// real one.
 int choose_mul_variant(sp_ctx *c, Lane &L, int db_id, const Db &db, const QDesc *qd, int nq, int *variant) {
-    if (nq < 2 || !db_mul_batch_supported(db.L)) {
-        *variant = 1;
+    if (c->mul_force && variant_available(c, L, db, nq, c->mul_force)) {
+        *variant = c->mul_force;
         return SP_OK;
     }
-    if (c->mul_force) {
-        *variant = c->mul_force;
+    if (nq < 2) {
+        *variant = 1;
         return SP_OK;
     }
     auto key = std::make_pair(db_id, nq);
     auto it = c->mul_choice.find(key);
-    if (it != c->mul_choice.end()) {
+    if (it != c->mul_choice.end() && variant_available(c, L, db, nq, it->second)) {
         *variant = it->second;
         return SP_OK;
     }
-    cudaEvent_t e[3];
-    for (auto &x : e) CU(cudaEventCreate(&x));
-    cudaError_t err = cudaEventRecord(e[0], L.st);
-    if (!err) err = launch_db_mul(db.d, db.L, qd, nq, L.d_err, L.st);
-    if (!err) err = cudaEventRecord(e[1], L.st);
-    if (!err) err = launch_db_mul_batch(db.d, db.L, qd, nq, L.st);
-    if (!err) err = cudaEventRecord(e[2], L.st);
-    if (!err) err = cudaEventSynchronize(e[2]);
-    float a = 0, b = 0;
-    if (!err) err = cudaEventElapsedTime(&a, e[0], e[1]);
-    if (!err) err = cudaEventElapsedTime(&b, e[1], e[2]);
-    for (auto &x : e) cudaEventDestroy(x);
-    if (err) return fail(SP_ERR_CUDA, std::string("multiply autotune: ") + cudaGetErrorString(err));
-    *variant = b < a ? 2 : 1;
-    c->mul_choice[key] = *variant;
+    int best = 1;
+    float best_ms = 0;
+    for (int v = 1; v <= 3; v++) {
+        if (!variant_available(c, L, db, nq, v)) continue;
+        cudaEvent_t e[2];
+        for (auto &x : e) CU(cudaEventCreate(&x));
+        cudaError_t err = cudaEventRecord(e[0], L.st);
+        if (!err) err = launch_mul_variant(L, db, qd, nq, v);
+        if (!err) err = cudaEventRecord(e[1], L.st);
+        if (!err) err = cudaEventSynchronize(e[1]);
+        float ms = 0;
+        if (!err) err = cudaEventElapsedTime(&ms, e[0], e[1]);
+        for (auto &x : e) cudaEventDestroy(x);
+        if (err) return fail(SP_ERR_CUDA, std::string("multiply autotune: ") + cudaGetErrorString(err));
+        if (v == 1 || ms < best_ms) {
+            best = v;
+            best_ms = ms;
+        }
+    }
+    *variant = best;
+    c->mul_choice[key] = best;
     return SP_OK;
 }
 
@@ -404,10 +460,8 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot)
         const Db &db = c->dbs.at(db_of_slot[i]);
         int variant = 1;
         TRY(choose_mul_variant(c, L, db_of_slot[i], db, L.d_qd + i, j - i, &variant));
-        if (variant == 2)
-            CU(launch_db_mul_batch(db.d, db.L, L.d_qd + i, j - i, st));
-        else
-            CU(launch_db_mul(db.d, db.L, L.d_qd + i, j - i, L.d_err, st));
+        CU(launch_mul_variant(L, db, L.d_qd + i, j - i, variant));
+        c->stats.db_mul_by_variant[variant - 1]++;
         launches++;
         mul_calls++;
         mul_bytes += db.L.words * 8 + (uint64_t)(j - i) * ((uint64_t)db.L.rows * D * 16 +
@@ -578,10 +632,9 @@ static int db_check_shape(sp_ctx *c, int nu1, int nu2) {
         return fail(SP_ERR_UNSUPPORTED, "t_gsw*nu2 GSW-bit encodings do not fit the odd expansion outputs "
                                         "(needs 2^nu1 >= t_gsw*nu2)");
     DbLayout L = make_db_layout(c->sp.T, nu1, nu2);
-    const int tcg = L.T * L.cg;
-    if (tcg != 4 && tcg != 8 && tcg != 16)
-        return fail(SP_ERR_UNSUPPORTED, "database shape has fewer than 4 polynomials per tile row");
-    if (L.rows > 128 && L.rows % 128) return fail(SP_ERR_UNSUPPORTED, "rows must be a multiple of 128");
+    // an image unit (rows x combo block) must be a whole number of 16-byte
+    // copy granules
+    if ((uint64_t)L.rows * L.cb < 4) return fail(SP_ERR_UNSUPPORTED, "database smaller than 4 residues per unit");
     return SP_OK;
 }
 
@@ -903,7 +956,7 @@ int sp_fetch_response(sp_ctx *c, int32_t slot, uint8_t *response, uint64_t respo
 
 int sp_set_db_mul_variant(sp_ctx *c, int32_t variant) {
     if (!c) return fail(SP_ERR_INVALID, "NULL context");
-    if (variant < 0 || variant > 2) return fail(SP_ERR_INVALID, "variant must be 0 (auto), 1 or 2");
+    if (variant < 0 || variant > 3) return fail(SP_ERR_INVALID, "variant must be 0 (auto), 1, 2 or 3");
     std::lock_guard<std::mutex> lk(c->mu);
     c->mul_force = variant;
     return SP_OK;
@@ -932,8 +985,12 @@ int sp_time_db_mul(sp_ctx *c, int32_t db_id, int32_t nq, int32_t iters, double *
     if (nq < 1 || nq > L.staged || iters < 1) return fail(SP_ERR_INVALID, "nq/iters out of range");
     for (int k = 0; k < nq; k++)
         if (L.slots[k].db != db_id) return fail(SP_ERR_INVALID, "staged slots must query this database");
+    int variant = c->mul_force ? c->mul_force : 1;
+    if (!variant_available(c, L, di->second, nq, variant))
+        return fail(SP_ERR_UNSUPPORTED, "multiply variant " + std::to_string(variant) +
+                                            " is not available for this database and query count");
     CU(cudaEventRecord(L.ev[0], L.st));
-    for (int i = 0; i < iters; i++) CU(launch_db_mul(di->second.d, di->second.L, L.d_qd, nq, L.d_err, L.st));
+    for (int i = 0; i < iters; i++) CU(launch_mul_variant(L, di->second, L.d_qd, nq, variant));
     CU(cudaEventRecord(L.ev[1], L.st));
     TRY(check_device_err(c, L));
     float ms = 0;
@@ -1127,6 +1184,47 @@ int sp_db_mul(sp_ctx *c, int32_t db_id, const uint64_t *sel, uint64_t *acc) {
     CU(launch_widen(o.as<uint32_t>(), w.as<uint64_t>(), acc_words / D, false, c->st));
     CU(cudaMemcpyAsync(acc, w.p, acc_words * 8, cudaMemcpyDeviceToHost, c->st));
     TRY(check_device_err(c, c->main));
+    return SP_OK;
+}
+
+int sp_db_mul_batch(sp_ctx *c, int32_t db_id, int32_t nq, const uint64_t *sel, uint64_t *acc) {
+    if (!c || !sel || !acc) return fail(SP_ERR_INVALID, "NULL argument");
+    if (nq < 1 || nq > 1024) return fail(SP_ERR_INVALID, "nq must be in [1, 1024]");
+    std::lock_guard<std::mutex> lk(c->mu);
+    auto di = c->dbs.find(db_id);
+    if (di == c->dbs.end()) return fail(SP_ERR_NOT_FOUND, "unknown database id");
+    const Db &db = di->second;
+    const DbLayout &L = db.L;
+    const uint64_t sel_words = (uint64_t)L.rows * 4 * D;
+    const uint64_t acc_words = (uint64_t)L.T * L.cols * 4 * D;
+    Tmp a(c), s(c), o(c), w(c), qd(c);
+    TRY(a.get(sel_words * 8));
+    TRY(s.get(sel_words * 4 * nq));
+    TRY(o.get(acc_words * 4 * nq));
+    TRY(w.get(acc_words * 8));
+    TRY(qd.get(sizeof(QDesc) * nq));
+    std::vector<QDesc> d(nq);
+    for (int q = 0; q < nq; q++) {
+        d[q] = QDesc{};
+        d[q].sel = s.as<uint32_t>() + sel_words * q;
+        d[q].acc = o.as<uint32_t>() + acc_words * q;
+        d[q].nu1 = L.nu1;
+        d[q].nu2 = L.nu2;
+        d[q].active = 1;
+        CU(cudaMemcpyAsync(a.p, sel + sel_words * q, sel_words * 8, cudaMemcpyHostToDevice, c->st));
+        CU(launch_sel_import(a.as<uint64_t>(), d[q].sel, L.rows, c->st));
+    }
+    CU(cudaMemcpyAsync(qd.p, d.data(), sizeof(QDesc) * nq, cudaMemcpyHostToDevice, c->st));
+    int variant = 1;
+    TRY(choose_mul_variant(c, c->main, db_id, db, qd.as<QDesc>(), nq, &variant));
+    CU(launch_mul_variant(c->main, db, qd.as<QDesc>(), nq, variant));
+    for (int q = 0; q < nq; q++) {
+        CU(launch_widen(d[q].acc, w.as<uint64_t>(), acc_words / D, false, c->st));
+        CU(cudaMemcpyAsync(acc + acc_words * q, w.p, acc_words * 8, cudaMemcpyDeviceToHost, c->st));
+        CU(cudaStreamSynchronize(c->st));
+    }
+    TRY(check_device_err(c, c->main));
+    c->stats.db_mul_by_variant[variant - 1]++;
     return SP_OK;
 }
 

@@ -8,23 +8,27 @@
 
 namespace sp {
 
-// Tiled device layout of one database (packed u64 = residue q1 | residue q2 << 32):
-//   [z_tile][col_group][row][t][c][z_in_tile]
-// z_tile = z / ZT, col = col_group*cg + c, t < T (plaintext polynomial of the
-// record).  A (z_tile, col_group) pair is one contiguous stream of
-// rows * T*cg*ZT words, consumed front to back by one CTA of the multiply.
+// Device layout of one database image: one u32 residue per (prime, combo,
+// row, slot), where combo m = t*cols + col enumerates the n*n plaintext
+// polynomials of every column:
+//   [prime][z][combo block][row][combo in block]
+// A block holds cb = min(128, combos) combos.  Each (prime, z, block) triple
+// ("unit") is one contiguous stream of rows*cb residues: the first-dimension
+// multiply for one slot and prime is the matrix product of that rows x cb
+// block with the query selectors of the slot, so a unit is also exactly the
+// operand tile of the tensor-core multiply (128 combos x rows).
 struct DbLayout {
     int T;        // n*n
     int nu1, nu2;
     int rows, cols;
-    int cg;       // columns per group
-    int ncg;      // cols / cg
-    int zt;       // z tile (64)
-    int nzt;      // D / zt
-    uint64_t words;  // total u64 words
-    __host__ __device__ uint64_t offset(int t, int row, int col, int z) const {
-        int zti = z / zt, zi = z % zt, g = col / cg, c = col % cg;
-        return ((((uint64_t)(zti * ncg + g) * rows + row) * T + t) * cg + c) * zt + zi;
+    int combos;   // T*cols
+    int cb;       // combos per block
+    int ncb;      // combos / cb
+    uint64_t words;  // u64 words (two residues each) = rows*combos*D
+    __host__ __device__ uint64_t units() const { return 2ull * D * ncb; }
+    __host__ __device__ uint64_t unit_words32() const { return (uint64_t)rows * cb; }
+    __host__ __device__ uint64_t offset32(int prime, int m, int row, int z) const {
+        return ((((uint64_t)prime * D + z) * ncb + m / cb) * rows + row) * cb + (m % cb);
     }
 };
 
@@ -59,6 +63,9 @@ struct StageParams {
 };
 
 
+// Multiprocessor count of the current device.
+int sm_count();
+
 // Twiddle tables (device, one set per context).
 void build_twiddles_host(TwiddleSet *host);
 
@@ -76,23 +83,33 @@ cudaError_t launch_ntt_planes(uint32_t *a, int count, bool inverse, const Twiddl
 cudaError_t launch_automorph(const uint64_t *in, uint64_t *out, int count, uint32_t t,
                              cudaStream_t st);
 
-// u8 records [n_rec][T][D] (record = row*cols + col) -> tiled database image
+// u8 records [n_rec][T][D] (record = row*cols + col) -> database image
 cudaError_t launch_db_encode(const uint8_t *records, uint64_t rec_begin, uint64_t rec_count,
-                             int pt_bits, const DbLayout &L, uint64_t *db, const TwiddleSet *tw,
+                             int pt_bits, const DbLayout &L, uint32_t *db, const TwiddleSet *tw,
                              cudaStream_t st);
-// NTT-form u32 planes [T][cols][rows][2][D] -> tiled image
-cudaError_t launch_db_import(const uint32_t *planes, const DbLayout &L, uint64_t *db,
+// NTT-form u32 planes [T][cols][rows][2][D] -> database image
+cudaError_t launch_db_import(const uint32_t *planes, const DbLayout &L, uint32_t *db,
                              cudaStream_t st);
 
 // First-dimension multiply for the `nq` queries qd[0..nq) against one
 // database: reads qd[q].sel (u32[rows][D][4], row0 q1, row0 q2, row1 q1,
 // row1 q2) and writes qd[q].acc (u32[T][cols][2 rows][2][D]), canonical.
-cudaError_t launch_db_mul(const uint64_t *db, const DbLayout &L, const QDesc *qd, int nq, int *err,
+// Streams the image once per query (bandwidth-bound variant).
+cudaError_t launch_db_mul(const uint32_t *db, const DbLayout &L, const QDesc *qd, int nq, int *err,
                           cudaStream_t st);
-int db_mul_ctas(const DbLayout &L);
-// Same result as launch_db_mul for nq > 1 queries, reading each database
-// word once per group of 4 queries (compute-bound variant).
+// Same result, reading each database residue once per group of 8 queries
+// on the integer pipe (compute-bound variant).
 bool db_mul_batch_supported(const DbLayout &L);
-cudaError_t launch_db_mul_batch(const uint64_t *db, const DbLayout &L, const QDesc *qd, int nq, cudaStream_t st);
+cudaError_t launch_db_mul_batch(const uint32_t *db, const DbLayout &L, const QDesc *qd, int nq, cudaStream_t st);
+
+// Tensor-core variant (tcgen05, exact fp16 limb products): the selectors of
+// up to TC_MAX_Q queries are first split into limb tiles in `limbs`
+// (tc_limb_bytes(L) bytes), then each unit of the image is multiplied by
+// them with fp32 accumulation in tensor memory.
+constexpr int TC_MAX_Q = 32;
+bool db_mul_tc_supported(const DbLayout &L);
+uint64_t tc_limb_bytes(const DbLayout &L);
+cudaError_t launch_db_mul_tc(const uint32_t *db, const DbLayout &L, const QDesc *qd, int nq, uint8_t *limbs,
+                             int *err, cudaStream_t st);
 
 }  // namespace sp

@@ -38,10 +38,13 @@ class SpStats(ctypes.Structure):
                 ("ms_expand", ctypes.c_double), ("ms_convert", ctypes.c_double),
                 ("ms_db_mul", ctypes.c_double), ("ms_fold", ctypes.c_double),
                 ("ms_pack", ctypes.c_double), ("ms_total", ctypes.c_double),
-                ("db_mul_calls", ctypes.c_uint64), ("db_mul_bytes", ctypes.c_uint64)]
+                ("db_mul_calls", ctypes.c_uint64), ("db_mul_bytes", ctypes.c_uint64),
+                ("db_mul_by_variant", ctypes.c_uint64 * 3)]
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["db_mul_by_variant"] = list(self.db_mul_by_variant)
+        return d
 
 
 class SpRequest(ctypes.Structure):
@@ -90,6 +93,7 @@ _SIGS = {
     "sp_regev_to_gsw": [_P, _I, _P, _I, _P],
     "sp_gsw_neg": [_P, _P, _I, _P],
     "sp_db_mul": [_P, _I, _P, _P],
+    "sp_db_mul_batch": [_P, _I, _I, _P, _P],
     "sp_fold": [_P, _P, _P, _I, _I, _P],
     "sp_fold_noalloc": [_P, _P, _P, _I, _I, _P],
     "sp_pack": [_P, _I, _P, _P, _U64],
@@ -225,7 +229,8 @@ class SpiralGPU:
         return resp
 
     def set_db_mul_variant(self, variant: int) -> None:
-        """0 = autotune, 1 = per-query streaming multiply, 2 = batched multiply."""
+        """0 = autotune, 1 = per-query streaming multiply, 2 = batched integer
+        multiply, 3 = tensor-core multiply."""
         _check(self.lib.sp_set_db_mul_variant(self.h, variant))
 
     def stats(self) -> dict:
@@ -286,6 +291,15 @@ class SpiralGPU:
         s = _u64(sel)
         out = np.empty((T, 1 << nu2, 2, 2, D), dtype=np.uint64)
         _check(self.lib.sp_db_mul(self.h, db_id, _ptr(s), _ptr(out)))
+        return out
+
+    def db_mul_batch(self, db_id: int, sels: np.ndarray, T: int, nu2: int) -> np.ndarray:
+        """sels [nq][2^nu1][2][2][D] -> [nq][T][2^nu2][2][2][D] with the forced
+        (or autotuned) multiply variant."""
+        s = _u64(sels)
+        nq = s.shape[0]
+        out = np.empty((nq, T, 1 << nu2, 2, 2, D), dtype=np.uint64)
+        _check(self.lib.sp_db_mul_batch(self.h, db_id, nq, _ptr(s), _ptr(out)))
         return out
 
     def fold(self, cts: np.ndarray, gsw: np.ndarray, nu2: int) -> np.ndarray:

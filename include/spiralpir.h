@@ -68,6 +68,7 @@ typedef struct sp_stats_out {
     double ms_total;         /* device time of whole answers */
     uint64_t db_mul_calls;   /* first-dimension multiply launches */
     uint64_t db_mul_bytes;   /* algorithmic bytes of those launches */
+    uint64_t db_mul_by_variant[3]; /* multiplies run by variant 1, 2, 3 */
 } sp_stats_out;
 
 /* One request of a batch. */
@@ -134,10 +135,14 @@ int sp_fetch_response(sp_ctx *ctx, int32_t slot, uint8_t *response, uint64_t res
 int sp_time_staged(sp_ctx *ctx, int32_t count, int32_t iters, double *ms_per_run);
 
 /* First-dimension multiply variant for launches with several queries on one
- * database: 0 = autotune (default: time both once per database and batch
- * size, keep the faster), 1 = per-query streaming kernel (TMA-fed, HBM-bound),
- * 2 = batched kernel (each database word read once per 4 queries).  The
- * result is identical. */
+ * database: 0 = autotune (default: time every available variant once per
+ * database and batch size, keep the fastest), 1 = per-query streaming kernel
+ * (TMA-fed, HBM-bound), 2 = batched integer kernel (each residue read once per
+ * 8 queries), 3 = tensor-core kernel (exact fp16 digit products, up to 32
+ * queries per pass; needs 128 combos per block and at most 512 rows, and a
+ * workspace of rows * 2 MiB per pipeline lane).  A forced variant that does
+ * not apply falls back to the autotuner.  sp_time_db_mul times the forced
+ * variant (1 when none is forced).  The result is identical. */
 int sp_set_db_mul_variant(sp_ctx *ctx, int32_t variant);
 /* Serving loop (continuous batching).  sp_serve_start starts a worker thread
  * with `lanes` pipeline lanes (each its own stream and max_batch workspace
@@ -187,6 +192,11 @@ int sp_gsw_neg(sp_ctx *ctx, const uint64_t *gsw, int32_t count, uint64_t *neg);
 /* First-dimension multiply (db_mul_kernel, gpu-pir/db_mul.cuh:26-70):
  *   sel uint64[2^nu1][2][2][D] -> acc uint64[n*n][2^nu2][2][2][D] */
 int sp_db_mul(sp_ctx *ctx, int32_t db_id, const uint64_t *sel, uint64_t *acc);
+/* The same multiply for `nq` selector sets in one launch, by the variant
+ * that sp_set_db_mul_variant forces (autotuned when none):
+ *   sel uint64[nq][2^nu1][2][2][D] -> acc uint64[nq][n*n][2^nu2][2][2][D]
+ * No counterpart in the reference (its multiply test runs one query). */
+int sp_db_mul_batch(sp_ctx *ctx, int32_t db_id, int32_t nq, const uint64_t *sel, uint64_t *acc);
 /* Fold (FOLD_CIPHERTEXTS, gpu-pir/folding.cuh:45-65) of T instances:
  *   cts uint64[T][2^nu2][2][D] raw, gsw uint64[nu2][2][2*t_gsw][2][D]
  *   -> out uint64[T][2][D] raw.  (G - C is derived, not passed.) */

@@ -147,6 +147,69 @@ def test_db_mul_extreme_values(gpu):
     gpu.unload_db(8)
 
 
+def _extreme_planes(shape, p, rng):
+    """uint32 residues mod p mixing the digit-decomposition edge cases
+    (0, 1, (p-1)/2, (p+1)/2, p-1) with uniform values."""
+    edge = np.array([0, 1, (p - 1) // 2, (p + 1) // 2, p - 1], dtype=np.uint32)
+    x = rng.integers(0, p, size=shape, dtype=np.uint32)
+    pick = rng.integers(0, 8, size=shape)
+    sel = pick < 5
+    x[sel] = edge[pick[sel]]
+    return x
+
+
+@pytest.mark.parametrize("variant", [1, 2, 3])
+def test_db_mul_batch_variants_extreme(gpu, variant):
+    """512 rows (the exactness bound of the tensor-core digit products) with
+    edge-case residues in the database and the selectors: every multiply
+    variant equals the oracle."""
+    T, nu1, nu2, nq = 4, 9, 5, 3
+    rng = np.random.default_rng(11)
+    db = np.empty((T, 1 << nu2, 1 << nu1, 2, D), dtype=np.uint32)
+    db[..., 0, :] = _extreme_planes(db[..., 0, :].shape, O.Q1, rng)
+    db[..., 1, :] = _extreme_planes(db[..., 1, :].shape, O.Q2, rng)
+    sels = np.empty((nq, 1 << nu1, 2, 2, D), dtype=np.uint32)
+    sels[..., 0, :] = _extreme_planes(sels[..., 0, :].shape, O.Q1, rng)
+    sels[..., 1, :] = _extreme_planes(sels[..., 1, :].shape, O.Q2, rng)
+    sels[0, :, :, 0, :] = (O.Q1 - 1) // 2       # all-extreme selector against the edge-heavy image
+    sels[0, :, :, 1, :] = (O.Q2 + 1) // 2
+    gpu.load_db_ntt(9, db, nu1, nu2)
+    try:
+        gpu.set_db_mul_variant(variant)
+        gpu.stats_reset()
+        got = gpu.db_mul_batch(9, sels, T, nu2).astype(np.uint32)
+        assert gpu.stats()["db_mul_by_variant"][variant - 1] == 1
+    finally:
+        gpu.set_db_mul_variant(0)
+        gpu.unload_db(9)
+    for q in range(nq):
+        assert np.array_equal(got[q], O.db_mul(db, sels[q], T, nu1, nu2)), f"query {q}"
+
+
+def test_db_mul_tc_two_passes(gpu):
+    """40 queries: the tensor-core multiply runs passes of 32 and 8 queries
+    (N = 64 and N = 16); every output equals the per-query kernel's."""
+    T, nu1, nu2, nq = 4, 7, 5, 40
+    rng = np.random.default_rng(12)
+    db = np.empty((T, 1 << nu2, 1 << nu1, 2, D), dtype=np.uint32)
+    db[..., 0, :] = rng.integers(0, O.Q1, size=db[..., 0, :].shape, dtype=np.uint32)
+    db[..., 1, :] = rng.integers(0, O.Q2, size=db[..., 1, :].shape, dtype=np.uint32)
+    sels = np.empty((nq, 1 << nu1, 2, 2, D), dtype=np.uint32)
+    sels[..., 0, :] = rng.integers(0, O.Q1, size=sels[..., 0, :].shape, dtype=np.uint32)
+    sels[..., 1, :] = rng.integers(0, O.Q2, size=sels[..., 1, :].shape, dtype=np.uint32)
+    gpu.load_db_ntt(9, db, nu1, nu2)
+    try:
+        gpu.set_db_mul_variant(3)
+        tc = gpu.db_mul_batch(9, sels, T, nu2)
+        gpu.set_db_mul_variant(1)
+        ref = gpu.db_mul_batch(9, sels, T, nu2)
+    finally:
+        gpu.set_db_mul_variant(0)
+        gpu.unload_db(9)
+    assert np.array_equal(tc, ref)
+    assert np.array_equal(ref[39].astype(np.uint32), O.db_mul(db, sels[39], T, nu1, nu2))
+
+
 def test_fold(gpu):
     x = cases.inputs("fold")
     got = gpu.fold(x["cts"], x["V"], x["nu2"])

@@ -1,5 +1,5 @@
 """GPU tests of batching and the serving loop: every result is the same
-alone and in the mix (bit-exact), for both multiply variants, for queries
+alone and in the mix (bit-exact), for every multiply variant, for queries
 submitted concurrently from several threads against databases of different
 shapes, and requests that cannot run complete with their error."""
 import threading
@@ -92,10 +92,11 @@ def test_serving_poisson_and_errors(world):
     assert res["p99_ms"] >= res["p50_ms"] > 0
 
 
-@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("variant", [1, 2, 3])
 def test_batch_many_columns(variant):
-    """nu2 = 10 (1024 columns, 256 column groups): batched multiply grid and
-    10 fold levels; each result decodes and equals the query answered alone."""
+    """nu2 = 10 (1024 columns, 32 blocks of 128 combos): batched multiply grids
+    and 10 fold levels; each result decodes and equals the query answered
+    alone."""
     p = P.PARAMS
     sh = P.DbShape(7, 10)
     recs = C.random_records(sh, p, seed=91)
@@ -109,7 +110,9 @@ def test_batch_many_columns(variant):
         for i, r in zip(idx, alone):
             assert np.array_equal(cl.decode(r), recs[i])
         gpu.set_db_mul_variant(variant)
+        gpu.stats_reset()
         batch = gpu.answer_batch([(1, 1, q) for q in qs])
+        assert gpu.stats()["db_mul_by_variant"][variant - 1] == 1
         for x, y in zip(batch, alone):
             assert np.array_equal(x, y)
 
