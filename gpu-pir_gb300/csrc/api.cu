@@ -95,8 +95,10 @@ struct Lane {
     cudaEvent_t ev[6]{};
     cudaEvent_t done = nullptr;
     int *d_err = nullptr;
-    uint8_t *limbs = nullptr;           // selector digit tiles of the tensor-core multiply
-    uint64_t limb_bytes = 0;
+    uint8_t *limbs = nullptr;           // tensor-core multiply workspace: selector digit
+    uint64_t limb_bytes = 0;            // tiles, then the chunk output
+    uint32_t *tc_out = nullptr;
+    uint64_t tc_out_bytes = 0;
     int cap = 0;
     int staged = 0;
     bool busy = false;                  // serving: a batch is in flight
@@ -297,6 +299,9 @@ void lane_free(sp_ctx *c, Lane &L) {
     release(c, L.limbs, L.limb_bytes);
     L.limbs = nullptr;
     L.limb_bytes = 0;
+    release(c, L.tc_out, L.tc_out_bytes);
+    L.tc_out = nullptr;
+    L.tc_out_bytes = 0;
     L.d_err = nullptr;
     L.d_qd = nullptr;
     if (L.h_qd) cudaFreeHost(L.h_qd);
@@ -345,21 +350,34 @@ int check_client_for(const sp_ctx *c, const Client &cl, const Db &db, int *need_
 }
 
 // Workspace of the tensor-core multiply for database layout `dl` (allocated
-// once per lane, under the HBM budget).  Returns false when it does not fit.
+// once per lane, grown when needed, under the HBM budget).  Returns false
+// when it does not fit.
 bool ensure_limbs(sp_ctx *c, Lane &L, const DbLayout &dl) {
-    const uint64_t need = tc_limb_bytes(dl);
-    if (L.limb_bytes >= need) return true;
-    if (L.limbs) {
+    const uint64_t need_l = tc_limb_bytes(dl), need_o = tc_out_bytes(dl);
+    if (L.limb_bytes >= need_l && L.tc_out_bytes >= need_o) return true;
+    if (L.limbs || L.tc_out) {
         if (cudaStreamSynchronize(L.st) != cudaSuccess) return false;
+    }
+    if (L.limb_bytes < need_l) {
         release(c, L.limbs, L.limb_bytes);
         L.limbs = nullptr;
         L.limb_bytes = 0;
+        if (alloc(c, (void **)&L.limbs, need_l) != SP_OK) {
+            g_err.clear();
+            return false;
+        }
+        L.limb_bytes = need_l;
     }
-    if (alloc(c, (void **)&L.limbs, need) != SP_OK) {
-        g_err.clear();
-        return false;
+    if (L.tc_out_bytes < need_o) {
+        release(c, L.tc_out, L.tc_out_bytes);
+        L.tc_out = nullptr;
+        L.tc_out_bytes = 0;
+        if (alloc(c, (void **)&L.tc_out, need_o) != SP_OK) {
+            g_err.clear();
+            return false;
+        }
+        L.tc_out_bytes = need_o;
     }
-    L.limb_bytes = need;
     return true;
 }
 
@@ -379,7 +397,7 @@ cudaError_t launch_mul_variant(Lane &L, const Db &db, const QDesc *qd, int nq, i
         case 3:
             for (int i = 0; i < nq; i += TC_MAX_Q) {
                 const int k = std::min(TC_MAX_Q, nq - i);
-                cudaError_t e = launch_db_mul_tc(db.d, db.L, qd + i, k, L.limbs, L.d_err, L.st);
+                cudaError_t e = launch_db_mul_tc(db.d, db.L, qd + i, k, L.limbs, L.tc_out, L.d_err, L.st);
                 if (e != cudaSuccess) return e;
             }
             return cudaSuccess;

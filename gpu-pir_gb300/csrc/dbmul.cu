@@ -7,6 +7,8 @@
 // copies (cp.async.bulk ... mbarrier::complete_tx) into a ring of stages.
 // Products of canonical residues (< 2^56) accumulate in 64-bit registers and
 // are reduced at least every 128 rows, which keeps the sums below 2^64.
+#include <type_traits>
+
 #include "async.cuh"
 #include "kernels.cuh"
 
@@ -106,7 +108,7 @@ namespace {
 
 constexpr int MUL_THREADS = 256;
 constexpr uint32_t MUL_STAGE_BYTES = 16384;
-constexpr int MUL_STAGES = 4;
+constexpr int MUL_STAGES = 2;
 constexpr int MUL_REDUCE = 128;  // own rows between reductions (sums < 2^64)
 
 __host__ __device__ inline int mul_stage_rows(const DbLayout &L) {
@@ -118,28 +120,42 @@ __host__ __device__ inline int mul_sel_bytes(const DbLayout &L) { return ((L.row
 
 }  // namespace
 
-// One CTA per (unit, query).  Thread (row phase rp, combo m) accumulates rows
-// r = rp (mod 256/cb) of combo m for both ciphertext rows; the phases are
-// summed through shared memory at the end.
+// Units per CTA: whole (prime, z) groups of ncb units, about 1 MiB of image
+// or more, so that pipeline start-up is paid rarely; at most 8 groups, which
+// leaves at least 2*D/8 = 512 CTAs per query.
+__host__ __device__ inline int mul_units_per_cta(const DbLayout &L) {
+    const uint64_t group = (uint64_t)L.ncb * L.unit_words32() * 4;
+    int k = 1;
+    while (group * k < (1u << 20) && k < 8) k <<= 1;
+    return L.ncb * k;
+}
+
+// One CTA per (run of units, query).  The run is one contiguous stream of
+// the image.  Thread (row phase rp, combo group mg) accumulates, for CPT
+// consecutive combos, rows r = rp (mod RS) for both ciphertext rows: one
+// 4*CPT-byte image load and one selector load feed 2*CPT independent
+// multiply-adds.  At the end of each unit the row phases are summed through
+// shared memory and the unit's outputs written.
+template <int CPT>
 __global__ void __launch_bounds__(MUL_THREADS) k_db_mul(const uint32_t *__restrict__ db, DbLayout L,
                                                         const QDesc *__restrict__ qd, int *err) {
+    using Vec = typename std::conditional<CPT == 4, uint4, uint32_t>::type;
     extern __shared__ __align__(128) uint8_t smem_mul[];
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem_mul);
     uint2 *ssel = reinterpret_cast<uint2 *>(smem_mul + 128);          // [rows] (ct row 0, ct row 1)
-    uint2 *red = reinterpret_cast<uint2 *>(smem_mul + 128 + mul_sel_bytes(L));   // [256]
-    uint8_t *stages = smem_mul + 128 + mul_sel_bytes(L) + MUL_THREADS * 8;
+    uint2 *red = reinterpret_cast<uint2 *>(smem_mul + 128 + mul_sel_bytes(L));   // [RS][cb]
+    uint8_t *stages = smem_mul + 128 + mul_sel_bytes(L) + MUL_THREADS * CPT * 8;
 
     const QDesc &Q = qd[blockIdx.y];
     const uint32_t *__restrict__ sel = Q.sel;
-    const uint64_t unit = blockIdx.x;
-    const int cbi = (int)(unit % L.ncb);
-    const int z = (int)((unit / L.ncb) % D);
-    const int prime = (int)(unit / ((uint64_t)L.ncb * D));
+    const int U = mul_units_per_cta(L);
+    const uint64_t u0 = (uint64_t)blockIdx.x * U;
     const int rows = L.rows, cb = L.cb;
     const int SR = mul_stage_rows(L);
+    const int SPU = rows / SR;                 // stages per unit
     const uint32_t stage_bytes = (uint32_t)SR * cb * 4;
-    const int n_iter = rows / SR;
-    const uint32_t *src = db + unit * L.unit_words32();
+    const int n_iter = U * SPU;
+    const uint32_t *src = db + u0 * L.unit_words32();
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < MUL_STAGES; s++) mbar_init(&bars[s], 1);
@@ -152,38 +168,73 @@ __global__ void __launch_bounds__(MUL_THREADS) k_db_mul(const uint32_t *__restri
     };
     if (threadIdx.x == 0)
         for (int s = 0; s < MUL_STAGES && s < n_iter; s++) issue(s, s);
-    // selectors of this slot and prime for every row (L2-resident gather)
-    for (int r = threadIdx.x; r < rows; r += MUL_THREADS) {
-        const uint32_t *sr = sel + ((uint64_t)r * D + z) * 4;
-        ssel[r] = make_uint2(__ldg(sr + prime), __ldg(sr + 2 + prime));
-    }
-    __syncthreads();
 
-    const int m = threadIdx.x % cb, rp = threadIdx.x / cb, RS = MUL_THREADS / cb;
-    const uint32_t p = prime ? QP1 : QP0;
-    const uint64_t mu = ~0ull / p;
-    uint64_t a0 = 0, a1 = 0;
+    const int groups = cb / CPT;               // threads per row
+    const int mg = threadIdx.x % groups, rp = threadIdx.x / groups, RS = MUL_THREADS / groups;
+    int prime = 0, z = 0;
+    uint32_t p = QP0;
+    uint64_t mu = ~0ull / QP0;
+    uint64_t a0[CPT], a1[CPT];
+#pragma unroll
+    for (int c = 0; c < CPT; c++) a0[c] = a1[c] = 0;
     int since = 0;
     bool ok = true;
     int it = 0;
     for (; it < n_iter; it++) {
         const int s = it % MUL_STAGES;
+        const int local = it % SPU, ui = it / SPU;
+        const uint64_t u = u0 + ui;
+        if (local == 0 && (ui == 0 || u % L.ncb == 0)) {
+            // new (prime, z): gather its selectors (L2-resident) for every row
+            z = (int)((u / L.ncb) % D);
+            prime = (int)(u / ((uint64_t)L.ncb * D));
+            p = prime ? QP1 : QP0;
+            mu = ~0ull / p;
+            for (int r = threadIdx.x; r < rows; r += MUL_THREADS) {
+                const uint32_t *sr = sel + ((uint64_t)r * D + z) * 4;
+                ssel[r] = make_uint2(__ldg(sr + prime), __ldg(sr + 2 + prime));
+            }
+            __syncthreads();
+        }
         // A thread whose wait runs out still computes (on stale data) so that
         // the whole CTA reaches the barrier below and leaves together.
         const bool arrived = mbar_wait_timed(&bars[s], (uint32_t)((it / MUL_STAGES) & 1));
-        const uint32_t *st = reinterpret_cast<const uint32_t *>(stages + s * MUL_STAGE_BYTES);
-        const uint2 *sv = ssel + it * SR;
+        const Vec *st = reinterpret_cast<const Vec *>(stages + s * MUL_STAGE_BYTES);
+        const uint2 *sv = ssel + local * SR;
 #pragma unroll 4
         for (int r = rp; r < SR; r += RS) {
-            const uint32_t d = st[r * cb + m];
+            const Vec d = st[r * groups + mg];
             const uint2 v = sv[r];
-            a0 += (uint64_t)v.x * d;
-            a1 += (uint64_t)v.y * d;
+            if constexpr (CPT == 4) {
+                a0[0] += (uint64_t)v.x * d.x;
+                a1[0] += (uint64_t)v.y * d.x;
+                a0[1] += (uint64_t)v.x * d.y;
+                a1[1] += (uint64_t)v.y * d.y;
+                a0[2] += (uint64_t)v.x * d.z;
+                a1[2] += (uint64_t)v.y * d.z;
+                a0[3] += (uint64_t)v.x * d.w;
+                a1[3] += (uint64_t)v.y * d.w;
+            } else {
+                a0[0] += (uint64_t)v.x * d;
+                a1[0] += (uint64_t)v.y * d;
+            }
         }
-        since += SR / RS;
+        since += (SR + RS - 1) / RS;
         if (since >= MUL_REDUCE) {
-            a0 = mod_u64_barrett(a0, p, mu);
-            a1 = mod_u64_barrett(a1, p, mu);
+#pragma unroll
+            for (int c = 0; c < CPT; c++) {
+                a0[c] = mod_u64_barrett(a0[c], p, mu);
+                a1[c] = mod_u64_barrett(a1[c], p, mu);
+            }
+            since = 0;
+        }
+        const bool last = local == SPU - 1;
+        if (last) {
+#pragma unroll
+            for (int c = 0; c < CPT; c++) {
+                red[rp * cb + mg * CPT + c] = make_uint2(mod_u64_barrett(a0[c], p, mu), mod_u64_barrett(a1[c], p, mu));
+                a0[c] = a1[c] = 0;
+            }
             since = 0;
         }
         // every thread is done with stage s; any timed-out wait ends the loop
@@ -192,42 +243,51 @@ __global__ void __launch_bounds__(MUL_THREADS) k_db_mul(const uint32_t *__restri
             break;
         }
         if (threadIdx.x == 0 && it + MUL_STAGES < n_iter) issue(it + MUL_STAGES, s);
+        if (last) {
+            if (threadIdx.x < 2 * cb) {
+                const int mm = threadIdx.x >> 1, k = threadIdx.x & 1;
+                uint64_t sum = 0;
+                for (int q = 0; q < RS; q++) {
+                    const uint2 v = red[q * cb + mm];
+                    sum += k ? v.y : v.x;
+                }
+                const uint64_t mgl = (u % L.ncb) * cb + mm;
+                Q.acc[((mgl * 2 + k) * 2 + prime) * D + z] = (uint32_t)(sum % p);
+            }
+            // `red` is rewritten at the end of the next unit
+            __syncthreads();
+        }
     }
     if (!ok) {
         // A copy never completed: report it, drain what is still in flight
-        // (bounded), and leave without writing results.
+        // (bounded), and leave without writing further results.
         if (threadIdx.x == 0) {
             atomicExch(err, 1);
             for (int k = it; k < n_iter && k < it + MUL_STAGES; k++)
                 mbar_wait_timed(&bars[k % MUL_STAGES], (uint32_t)((k / MUL_STAGES) & 1));
         }
         __syncthreads();
-        return;
     }
-    red[threadIdx.x] = make_uint2(mod_u64_barrett(a0, p, mu), mod_u64_barrett(a1, p, mu));
-    __syncthreads();
-    if (threadIdx.x < 2 * cb) {
-        const int mm = threadIdx.x >> 1, k = threadIdx.x & 1;
-        uint64_t s = 0;
-        for (int q = 0; q < RS; q++) {
-            const uint2 v = red[q * cb + mm];
-            s += k ? v.y : v.x;
-        }
-        const int mg = cbi * cb + mm;
-        Q.acc[(((uint64_t)mg * 2 + k) * 2 + prime) * D + z] = (uint32_t)(s % p);
-    }
+}
+
+template <int CPT>
+static cudaError_t launch_mul_cpt(const uint32_t *db, const DbLayout &L, const QDesc *qd, int nq, int *err,
+                                  cudaStream_t st) {
+    const uint64_t ctas = L.units() / mul_units_per_cta(L);
+    if (ctas * mul_units_per_cta(L) != L.units() || ctas > 0x7fffffffull) return cudaErrorInvalidValue;
+    const int smem = 128 + mul_sel_bytes(L) + MUL_THREADS * CPT * 8 + MUL_STAGES * MUL_STAGE_BYTES;
+    cudaError_t e = cudaFuncSetAttribute(k_db_mul<CPT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid((unsigned)ctas, nq);
+    k_db_mul<CPT><<<grid, MUL_THREADS, smem, st>>>(db, L, qd, err);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_db_mul(const uint32_t *db, const DbLayout &L, const QDesc *qd, int nq, int *err,
                           cudaStream_t st) {
-    if (L.rows % mul_stage_rows(L) != 0 || MUL_THREADS % L.cb != 0 || L.units() > 0x7fffffffull)
-        return cudaErrorInvalidValue;
-    const int smem = 128 + mul_sel_bytes(L) + MUL_THREADS * 8 + MUL_STAGES * MUL_STAGE_BYTES;
-    cudaError_t e = cudaFuncSetAttribute(k_db_mul, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    dim3 grid((unsigned)L.units(), nq);
-    k_db_mul<<<grid, MUL_THREADS, smem, st>>>(db, L, qd, err);
-    return cudaGetLastError();
+    if (L.rows % mul_stage_rows(L) != 0 || MUL_THREADS % L.cb != 0) return cudaErrorInvalidValue;
+    if (L.cb >= 4) return launch_mul_cpt<4>(db, L, qd, nq, err, st);
+    return launch_mul_cpt<1>(db, L, qd, nq, err, st);
 }
 
 // ------------------------------------------------------- batched multiply

@@ -14,23 +14,37 @@
 // exactly.  The epilogue returns sum_d C_d * (2^(7d) mod p) reduced mod p,
 // bit-identical to the integer-pipe multiplies.
 //
-// Layout of the work (tcgen05, cta_group::1, kind::f16, M = 128, N = 2B
-// rounded up to 16 (<= 64), K = 16 per instruction):
-//  * A = database digits, 128 combos x 32 rows per stage, K-major canonical
-//    (no swizzle: 8x8 core matrices of 128 B, SBO = 128 B between 8-combo
-//    groups, LBO = 2 KiB between 8-row groups), written to shared memory by
-//    the converter warps from the u32 image;
-//  * B = selector digits, prepared once per batch by k_tc_limbs in the same
-//    canonical form (SBO = 128 B, LBO = N*16 B) and fetched per stage with one
-//    1-D bulk TMA copy;
-//  * D = seven accumulators of N fp32 columns each in tensor memory (7*64 =
-//    448 of the 512 columns).
-// Warp roles of the persistent CTA (one per SM; 168 KiB of shared memory
+// Layout of the work (tcgen05, cta_group::1, kind::f16, M = 128, K = 16 per
+// instruction; N = 2B rounded up to 16, at most 64, selector columns):
+//  * A = database digits, 128 combos x 16 rows per K-step, in tensor memory:
+//    lane = combo, 8 columns of fp16 pairs (rows 2c, 2c+1) per digit.  The
+//    converter warps write them with tcgen05.st from the u32 image rows that
+//    the producer stages in shared memory; two K-step buffers of 32 columns;
+//  * B = the four selector digits side by side, 4N columns (digit j in
+//    columns jN .. jN+N-1), prepared once per batch by k_tc_limbs in the
+//    K-major canonical shared-memory form (no swizzle: 8x8 core matrices of
+//    128 B, SBO = 128 B between 8-column groups, LBO = 4N*16 B between 8-row
+//    groups) and fetched per stage with one 1-D bulk TMA copy;
+//  * D = seven accumulators C_0..C_6 of N fp32 columns each, adjacent (7*64 =
+//    448 columns); with the A buffers (64 columns) that fills the 512
+//    columns of tensor memory.
+// One instruction per A digit i and K-step: A_i x [B_0 B_1 B_2 B_3] (N' = 4N,
+// 256 at N = 64) into columns iN .. iN+4N-1, i.e. A_i B_j lands in C_(i+j):
+// the weight classes are summed by the tensor core itself.  The columns of
+// consecutive instructions overlap, so every instruction accumulates and the
+// accumulators are zeroed as they are read.
+// Tensor memory holds one accumulator set, so the MMAs of the next unit wait
+// until the current one is drained; all sixteen converter and epilogue warps
+// drain it (each lane quarter by four warps, each a quarter of the columns).
+// Warp roles of the persistent CTA (one per SM; the shared-memory footprint
 // keeps it alone on its SM, so its 512-column TMEM allocation never waits):
-//   warp 0      TMA producer of the selector stages
-//   warp 1      TMEM allocation, MMA issue (one thread), TMEM release
-//   warps 2..5  converters: image residues -> digit tiles
-//   warps 6..9  epilogue: TMEM -> registers -> mod p -> accumulator planes
+//   warp 0       TMA producer of the selector stages and of the image rows
+//   warp 1       TMEM allocation, MMA issue (one thread), TMEM release
+//   warps 2..9   converters: image rows -> digit pairs -> tensor memory
+//                (warps 2..5 even K-steps, 6..9 odd; lane = combo)
+//                then their share of the drain
+//   warps 10..17 drain: TMEM -> registers -> mod p -> chunk output
+// Queries beyond 32 run as further passes over the image.
 // Every barrier wait is bounded in time; a wait that runs out sets an error
 // flag, the other roles stop at their next wait, in-flight copies and MMAs
 // are drained (bounded), the TMEM is released and the kernel returns.
@@ -43,29 +57,33 @@ namespace sp {
 namespace {
 
 constexpr int TC_M = 128;
-constexpr int TC_KC = 32;                     // rows per stage
-constexpr int TC_NA = 3;                      // digit-tile (A) stages
-constexpr int TC_NS = 4;                      // selector (B) stages
+constexpr int TC_KC = 32;                     // rows per stage (two K-steps)
+constexpr int TC_NS = 6;                      // selector (B) stages
+constexpr int TC_ND = 6;                      // image (u32) stages
 constexpr int TC_MAX_N = 2 * TC_MAX_Q;        // 64
-constexpr uint32_t A_LIMB_BYTES = TC_M * TC_KC * 2;          // 8 KiB
-constexpr uint32_t A_STAGE_BYTES = 4 * A_LIMB_BYTES;         // 32 KiB
 constexpr uint32_t S_STAGE_MAX = 4 * TC_KC * TC_MAX_N * 2;   // 16 KiB
-constexpr uint32_t A_RING = 0;
-constexpr uint32_t S_RING = A_RING + TC_NA * A_STAGE_BYTES;  // 96 KiB
-constexpr uint32_t GUARD = 8192;
-constexpr uint32_t CTRL = S_RING + TC_NS * S_STAGE_MAX + GUARD;  // 168 KiB
+constexpr uint32_t D_STAGE_BYTES = TC_KC * TC_M * 4;         // 16 KiB
+constexpr uint32_t S_RING = 0;
+constexpr uint32_t D_RING = S_RING + TC_NS * S_STAGE_MAX;    // 96 KiB
+constexpr uint32_t CTRL = D_RING + TC_ND * D_STAGE_BYTES;    // 192 KiB
 constexpr uint32_t TC_SMEM = CTRL + 1024;
-constexpr int TC_THREADS = 320;
+constexpr int TC_THREADS = 576;
+constexpr int TC_CONV = 128;                  // converter threads per K-step parity
+constexpr int TC_DRAIN = 512;                 // converter + epilogue threads
 constexpr uint32_t TMEM_COLS = 512;
+constexpr uint32_t TMEM_A = 448;              // first column of the A buffers
 constexpr int32_t DIGIT_BIAS = 64 * (1 + 128 + 128 * 128);   // 1056832
+// 64 * (1 + 2^7 + 2^14 + 2^21): with it, all four offset digits are plain
+// bit fields of one non-negative word (bits 0-6, 7-13, 14-20, 21-28).
+constexpr uint32_t DIGIT_BIAS4 = 64u * (1u + 128u + 128u * 128u + 128u * 128u * 128u);   // 135274560
 
 struct Ctrl {
     uint64_t s_full[TC_NS], s_empty[TC_NS];
-    uint64_t a_full[TC_NA], a_empty[TC_NA];
+    uint64_t a_full[2], a_empty[2];
+    uint64_t d_full[TC_ND], d_empty[TC_ND];
     uint64_t acc_full, acc_empty, drain;
     uint32_t tmem_base;
     int abort;
-    uint32_t *acc[TC_MAX_Q];
 };
 static_assert(sizeof(Ctrl) <= 1024, "control block");
 
@@ -88,9 +106,28 @@ __device__ __forceinline__ uint32_t digit_pair(uint32_t ulo, uint32_t uhi) {
     return *reinterpret_cast<uint32_t *>(&h);
 }
 
-__device__ __forceinline__ void sts128(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
-    asm volatile("st.shared.v4.b32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d)
-                 : "memory");
+// Biased word of a canonical residue: centred value + DIGIT_BIAS4, in
+// [0, 2^29).  Its digit fields are the offset digits of digits4.
+__device__ __forceinline__ uint32_t biased(uint32_t x, uint32_t p) {
+    return x + (x > (p >> 1) ? DIGIT_BIAS4 - p : DIGIT_BIAS4);
+}
+
+__device__ __forceinline__ uint32_t hsub1088(uint32_t w) {
+    __half2 h = *reinterpret_cast<__half2 *>(&w);
+    h = __hsub2(h, __halves2half2(__ushort_as_half(0x6440), __ushort_as_half(0x6440)));
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+// The four fp16 digit pairs (digit l of ya, digit l of yb), l = 0..3, of two
+// biased words, with byte permutes instead of per-digit shifts.
+__device__ __forceinline__ void digit_pairs(uint32_t ya, uint32_t yb, uint32_t (&w)[4]) {
+    const uint32_t t0 = __byte_perm(ya, yb, 0x5410);   // bits 0-15 of each
+    const uint32_t t1 = __byte_perm(ya, yb, 0x6521);   // bits 8-23
+    const uint32_t t2 = __byte_perm(ya, yb, 0x7632);   // bits 16-31
+    w[0] = hsub1088((t0 & 0x007F007Fu) | 0x64006400u);
+    w[1] = hsub1088(((t0 >> 7) & 0x007F007Fu) | 0x64006400u);
+    w[2] = hsub1088(((t1 >> 6) & 0x007F007Fu) | 0x64006400u);
+    w[3] = hsub1088(((t2 >> 5) & 0x00FF00FFu) | 0x64006400u);
 }
 
 // tcgen05 shared-memory matrix descriptor, no swizzle.
@@ -104,14 +141,23 @@ __device__ __forceinline__ uint32_t instr_desc(int n) {
     return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
 }
 
-__device__ __forceinline__ void mma_f16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
-                                        uint32_t accumulate) {
+// D (tmem) (+)= A (tmem) * B (shared memory descriptor)
+__device__ __forceinline__ void mma_f16_ts(uint32_t tmem_d, uint32_t tmem_a, uint64_t bdesc, uint32_t idesc,
+                                           uint32_t accumulate) {
     asm volatile(
         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
-        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "r"(tmem_a), "l"(bdesc), "r"(idesc), "r"(accumulate)
         : "memory");
 }
+
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const uint32_t (&v)[8]) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr),
+                 "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7])
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 __device__ __forceinline__ void mma_commit(uint64_t *bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -126,24 +172,81 @@ __device__ __forceinline__ void tc_fence_before() {
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-        "%14, %15}, [%16];"
-        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-        : "r"(taddr));
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&v)[8]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+                 : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+                 : "r"(taddr));
 }
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
 }  // namespace
 
+// Exact fp32 integer -> int32 for |x| <= 2^22 with one add: the sum with
+// 1.5 * 2^23 holds x in its low mantissa bits (also at the +-2^22 ends).
+__device__ __forceinline__ int32_t f2i_small(uint32_t bits) {
+    return __float_as_int(__fadd_rn(__uint_as_float(bits), 12582912.0f)) - 0x4B400000;
+}
+
+// Drain one lane quarter of the accumulators for columns c0, c0 + 32, ...
+// (chunks of 8): read C_0..C_6, zero them, and write
+//   sum_d C_d 2^(7d) mod p
+// into the chunk output [prime][z - z0][n][combo].  |C_d| <= (pairs of
+// class d) * 2^21, so classes 0, 1, 5, 6 (at most 2 digit pairs) convert
+// with f2i_small and classes 2, 3, 4 with cvt.
+__device__ __forceinline__ void drain_quarter(uint32_t lane_addr, int N, int c0, const DbLayout &L, int z0,
+                                              int zc, uint64_t u, int m, uint32_t *out) {
+    const int cbi = (int)(u % L.ncb);
+    const int zl = (int)((u / L.ncb) % D) - z0;
+    const int prime = (int)(u / ((uint64_t)L.ncb * D));
+    const uint32_t p = prime ? QP1 : QP0;
+    const uint32_t npinv = 0u - (prime ? P1_PINV : P0_PINV);
+    // weights 2^(7d) * 2^32 mod p: one Montgomery reduction of the weighted
+    // sum returns sum_d C_d 2^(7d) mod p
+    int32_t w[7];
+    uint64_t wd = (1ull << 32) % p;
+#pragma unroll
+    for (int d = 0; d < 7; d++) {
+        w[d] = (int32_t)wd;
+        wd = (wd << 7) % p;
+    }
+    // a multiple of p above the largest |sum| (< 7 * 2^23 * 2^28)
+    const int64_t off = (int64_t)(((1ull << 54) / p + 1) * p);
+    const uint32_t mg = (uint32_t)cbi * TC_M + m;
+    uint32_t *o = out + ((uint64_t)prime * zc + zl) * N * L.combos + mg;
+    const uint32_t zero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int n0 = c0; n0 < N; n0 += 32) {
+        uint32_t v8[7][8];
+#pragma unroll
+        for (int d = 0; d < 7; d++) tmem_ld8(lane_addr + d * N + n0, v8[d]);
+        tmem_wait_ld();
+#pragma unroll
+        for (int d = 0; d < 7; d++) tmem_st8(lane_addr + d * N + n0, zero8);
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            int64_t sum = off;
+            sum += (int64_t)f2i_small(v8[0][c]) * w[0];
+            sum += (int64_t)f2i_small(v8[1][c]) * w[1];
+            sum += (int64_t)__float2int_rn(__uint_as_float(v8[2][c])) * w[2];
+            sum += (int64_t)__float2int_rn(__uint_as_float(v8[3][c])) * w[3];
+            sum += (int64_t)__float2int_rn(__uint_as_float(v8[4][c])) * w[4];
+            sum += (int64_t)f2i_small(v8[5][c]) * w[5];
+            sum += (int64_t)f2i_small(v8[6][c]) * w[6];
+            const uint64_t x = (uint64_t)sum;
+            const uint64_t t = x + (uint64_t)((uint32_t)x * npinv) * p;
+            uint32_t r = (uint32_t)(t >> 32);
+            r = r >= p ? r - p : r;
+            o[(uint64_t)(n0 + c) * L.combos] = r;     // a warp writes 128 contiguous bytes
+        }
+    }
+    tmem_wait_st();
+}
+
 // ------------------------------------------------------ selector digits
 // Thread (n, z, row group of 8): n = 2*query + ciphertext row.  Writes, for
-// both primes, the four digit planes of 8 consecutive rows as 16-byte rows of
-// the canonical K-major B tiles:
-//   limbs[prime][z][stage][digit][8-row group][N/8][8 n][8 rows]  (fp16)
+// both primes, the four digits of 8 consecutive rows as 16-byte rows of the
+// canonical K-major B tiles (column = digit*N + n):
+//   limbs[prime][z][stage][8-row group][digit][N/8][8 n][8 rows]  (fp16)
 __global__ void __launch_bounds__(256) k_tc_limbs(const QDesc *__restrict__ qd, int nq, int rows, int N,
                                                   uint8_t *__restrict__ limbs) {
     const uint64_t total = (uint64_t)N * D * (rows / 8);
@@ -182,7 +285,7 @@ __global__ void __launch_bounds__(256) k_tc_limbs(const QDesc *__restrict__ qd, 
                 w.y = digit_pair(u[2][l], u[3][l]);
                 w.z = digit_pair(u[4][l], u[5][l]);
                 w.w = digit_pair(u[6][l], u[7][l]);
-                const uint64_t off = ((uint64_t)(s * 4 + l) * 4 + kg) * (N / 8) * 128 + (n / 8) * 128 + (n % 8) * 16;
+                const uint64_t off = ((uint64_t)(s * 4 + kg) * 4 + l) * (N / 8) * 128 + (n / 8) * 128 + (n % 8) * 16;
                 *reinterpret_cast<uint4 *>(base + off) = w;
             }
         }
@@ -190,9 +293,18 @@ __global__ void __launch_bounds__(256) k_tc_limbs(const QDesc *__restrict__ qd, 
 }
 
 // ------------------------------------------------------------ multiply
-__global__ void __launch_bounds__(TC_THREADS, 1) k_db_mul_tc(const uint32_t *__restrict__ db, DbLayout L,
-                                                             const QDesc *__restrict__ qd, int nq, int N,
-                                                             const uint8_t *__restrict__ limbs, int *err) {
+// Units of one launch: both primes, slots [z0, z0 + zc), every combo block;
+// chunk-local index v -> image unit.
+__device__ __forceinline__ uint64_t chunk_unit(const DbLayout &L, int z0, int zc, uint64_t v) {
+    const uint64_t per_prime = (uint64_t)zc * L.ncb;
+    const uint64_t prime = v / per_prime, r = v % per_prime;
+    return (prime * D + z0 + r / L.ncb) * L.ncb + r % L.ncb;
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1) k_db_mul_tc(const uint32_t *__restrict__ db, DbLayout L, int nq,
+                                                             int N, int z0, int zc,
+                                                             const uint8_t *__restrict__ limbs,
+                                                             uint32_t *__restrict__ out, int *err) {
     extern __shared__ __align__(1024) uint8_t smem_tc[];
     Ctrl &C = *reinterpret_cast<Ctrl *>(smem_tc + CTRL);
     volatile int *abort = &C.abort;
@@ -201,24 +313,27 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_db_mul_tc(const uint32_t *__r
     const int rows = L.rows;
     const int S = rows / TC_KC;                        // stages per unit
     const uint32_t s_bytes = 4u * TC_KC * N * 2;       // selector stage bytes
-    const uint64_t units = L.units();
+    const uint64_t units = 2ull * zc * L.ncb;      // units of this launch
 
     if (threadIdx.x == 0) {
         for (int i = 0; i < TC_NS; i++) {
             mbar_init(&C.s_full[i], 1);
             mbar_init(&C.s_empty[i], 1);
         }
-        for (int i = 0; i < TC_NA; i++) {
-            mbar_init(&C.a_full[i], 128);
+        for (int i = 0; i < 2; i++) {
+            mbar_init(&C.a_full[i], TC_CONV);
             mbar_init(&C.a_empty[i], 1);
         }
+        for (int i = 0; i < TC_ND; i++) {
+            mbar_init(&C.d_full[i], 1);
+            mbar_init(&C.d_empty[i], 2 * TC_CONV);
+        }
         mbar_init(&C.acc_full, 1);
-        mbar_init(&C.acc_empty, 128);
+        mbar_init(&C.acc_empty, TC_DRAIN);
         mbar_init(&C.drain, 1);
         C.abort = 0;
         fence_mbar_init();
     }
-    if (threadIdx.x < TC_MAX_Q) C.acc[threadIdx.x] = threadIdx.x < nq ? qd[threadIdx.x].acc : nullptr;
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_addr(&C.tmem_base)),
@@ -233,66 +348,79 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_db_mul_tc(const uint32_t *__r
 
     if (warp == 0) {
         // ---------------------------------------------------- producer
+        // per stage: the selector digit tile (for the MMA) and the image
+        // rows (for the converters), each into its own ring
         if (lane == 0) {
             uint32_t G = 0;
             bool stop = false;
-            for (uint64_t u = blockIdx.x; u < units && !stop; u += gridDim.x) {
+            for (uint64_t v = blockIdx.x; v < units && !stop; v += gridDim.x) {
+                const uint64_t u = chunk_unit(L, z0, zc, v);
                 const uint64_t pz = u / L.ncb;        // prime*D + z
-                const uint8_t *src = limbs + pz * (uint64_t)rows * N * 8;
+                const uint8_t *sel_src = limbs + pz * (uint64_t)rows * N * 8;
+                const uint32_t *db_src = db + u * L.unit_words32();
                 for (int s = 0; s < S; s++, G++) {
-                    const int slot = G % TC_NS;
+                    const int ss = G % TC_NS, ds = G % TC_ND;
                     if (G >= (uint32_t)TC_NS &&
-                        !mbar_wait_bounded(&C.s_empty[slot], ((G / TC_NS) + 1) & 1, abort)) {
+                        !mbar_wait_bounded(&C.s_empty[ss], ((G / TC_NS) + 1) & 1, abort)) {
                         stop = true;
                         break;
                     }
-                    mbar_expect_tx(&C.s_full[slot], s_bytes);
-                    tma_bulk_g2s(smem_tc + S_RING + slot * S_STAGE_MAX, src + (uint64_t)s * s_bytes, s_bytes,
-                                 &C.s_full[slot]);
+                    mbar_expect_tx(&C.s_full[ss], s_bytes);
+                    tma_bulk_g2s(smem_tc + S_RING + ss * S_STAGE_MAX, sel_src + (uint64_t)s * s_bytes, s_bytes,
+                                 &C.s_full[ss]);
+                    if (G >= (uint32_t)TC_ND &&
+                        !mbar_wait_bounded(&C.d_empty[ds], ((G / TC_ND) + 1) & 1, abort)) {
+                        // the selector copy of this stage is in flight: count it
+                        G++;
+                        stop = true;
+                        break;
+                    }
+                    mbar_expect_tx(&C.d_full[ds], D_STAGE_BYTES);
+                    tma_bulk_g2s(smem_tc + D_RING + ds * D_STAGE_BYTES, db_src + (uint64_t)s * TC_KC * TC_M,
+                                 D_STAGE_BYTES, &C.d_full[ds]);
                 }
             }
             if (stop) {
                 // let the copies already issued land before the CTA can exit
-                for (uint32_t k = (G > (uint32_t)TC_NS ? G - TC_NS : 0); k < G; k++)
+                for (uint32_t k = (G > (uint32_t)TC_NS ? G - TC_NS : 0); k < G; k++) {
                     mbar_wait_timed(&C.s_full[k % TC_NS], (k / TC_NS) & 1);
+                    mbar_wait_timed(&C.d_full[k % TC_ND], (k / TC_ND) & 1);
+                }
             }
         }
     } else if (warp == 1) {
         // ---------------------------------------------------------- MMA
         if (lane == 0) {
-            const uint32_t idesc = instr_desc(N);
+            const uint32_t idesc = instr_desc(4 * N);
             uint32_t G = 0, ui = 0;
             bool stop = false;
-            for (uint64_t u = blockIdx.x; u < units && !stop; u += gridDim.x, ui++) {
-                if (ui > 0 && !mbar_wait_bounded(&C.acc_empty, (ui - 1) & 1, abort)) break;
+            for (uint64_t v = blockIdx.x; v < units && !stop; v += gridDim.x, ui++) {
+                // phase 0 of acc_empty: accumulators cleared at start;
+                // phase ui: unit ui - 1 drained
+                const uint32_t dacc = tmem;
+                if (!mbar_wait_bounded(&C.acc_empty, ui & 1, abort)) break;
                 tc_fence_after();
-                uint32_t inited = 0;
                 for (int s = 0; s < S; s++, G++) {
-                    const int as = G % TC_NA, ss = G % TC_NS;
-                    if (!mbar_wait_bounded(&C.a_full[as], (G / TC_NA) & 1, abort) ||
-                        !mbar_wait_bounded(&C.s_full[ss], (G / TC_NS) & 1, abort)) {
+                    const int ss = G % TC_NS;
+                    if (!mbar_wait_bounded(&C.s_full[ss], (G / TC_NS) & 1, abort)) {
                         stop = true;
                         break;
                     }
-                    tc_fence_after();
-                    const uint32_t a0 = sbase + A_RING + as * A_STAGE_BYTES;
                     const uint32_t b0 = sbase + S_RING + ss * S_STAGE_MAX;
 #pragma unroll
                     for (int ks = 0; ks < TC_KC / 16; ks++) {
-#pragma unroll
-                        for (int i = 0; i < 4; i++) {
-                            const uint64_t ad = smem_desc(a0 + i * A_LIMB_BYTES + ks * 2 * 2048, 2048, 128);
-#pragma unroll
-                            for (int j = 0; j < 4; j++) {
-                                const int d = i + j;
-                                const uint64_t bd =
-                                    smem_desc(b0 + j * (N * 64) + ks * 2 * (N * 16), (uint32_t)N * 16, 128);
-                                mma_f16(tmem + d * N, ad, bd, idesc, (inited >> d) & 1);
-                                inited |= 1u << d;
-                            }
+                        if (!mbar_wait_bounded(&C.a_full[ks], G & 1, abort)) {
+                            stop = true;
+                            break;
                         }
+                        tc_fence_after();
+                        const uint64_t bd = smem_desc(b0 + ks * 2 * (N * 64), (uint32_t)N * 64, 128);
+#pragma unroll
+                        for (int i = 0; i < 4; i++)
+                            mma_f16_ts(dacc + i * N, tmem + TMEM_A + 32 * ks + 8 * i, bd, idesc, 1);
+                        mma_commit(&C.a_empty[ks]);
                     }
-                    mma_commit(&C.a_empty[as]);
+                    if (stop) break;
                     mma_commit(&C.s_empty[ss]);
                 }
                 if (!stop) mma_commit(&C.acc_full);
@@ -301,86 +429,96 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_db_mul_tc(const uint32_t *__r
             mma_commit(&C.drain);
             mbar_wait_timed(&C.drain, 0);
         }
-    } else if (warp < 6) {
+    } else if (warp < 10) {
         // --------------------------------------------------- converters
-        const int m = threadIdx.x - 64;      // combo within the unit
-        const uint32_t sts_off = (m >> 3) * 128 + (m & 7) * 16;
-        uint32_t G = 0;
+        // warp quarter q4 owns TMEM lanes (= combos) 32*q4 .. 32*q4+31;
+        // h = 0 converts rows 0..15 of each stage (K-step 0), h = 1 rows 16..31
+        const int q4 = warp & 3, h = (warp - 2) >> 2;
+        const int m = q4 * 32 + lane;
+        const uint32_t lds_off = (h * 16 * TC_M + m) * 4;
+        const uint32_t ta0 = tmem + ((uint32_t)(q4 * 32) << 16) + TMEM_A + 32 * h;
+        const uint32_t lane_addr = tmem + ((uint32_t)(q4 * 32) << 16);
+        const int c0 = h * 8;                 // drain chunks h, h + 4, ...
+        {
+            // tensor memory is undefined after allocation: clear this warp's
+            // accumulator chunks before the first unit
+            const uint32_t zero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (int n0 = c0; n0 < N; n0 += 32)
+#pragma unroll
+                for (int d = 0; d < 7; d++) tmem_st8(lane_addr + d * N + n0, zero8);
+            tmem_wait_st();
+            tc_fence_before();
+            mbar_arrive(&C.acc_empty);
+        }
+        uint32_t G = 0, ui = 0;
         bool stop = false;
-        for (uint64_t u = blockIdx.x; u < units && !stop; u += gridDim.x) {
+        for (uint64_t v = blockIdx.x; v < units && !stop; v += gridDim.x, ui++) {
+            const uint64_t u = chunk_unit(L, z0, zc, v);
             const uint32_t p = (u / ((uint64_t)L.ncb * D)) ? QP1 : QP0;
-            const uint32_t *src = db + u * L.unit_words32() + m;
-            uint32_t xr[TC_KC];
-#pragma unroll
-            for (int j = 0; j < TC_KC; j++) xr[j] = __ldg(src + j * TC_M);
             for (int s = 0; s < S; s++, G++) {
-                uint32_t xn[TC_KC];
-                if (s + 1 < S) {
-#pragma unroll
-                    for (int j = 0; j < TC_KC; j++) xn[j] = __ldg(src + ((s + 1) * TC_KC + j) * TC_M);
-                }
-                const int as = G % TC_NA;
-                if (G >= (uint32_t)TC_NA && !mbar_wait_bounded(&C.a_empty[as], ((G / TC_NA) + 1) & 1, abort)) {
+                const int ds = G % TC_ND;
+                bool ok = mbar_wait_bounded(&C.d_full[ds], (G / TC_ND) & 1, abort);
+                if (!__all_sync(0xffffffffu, ok)) {
                     stop = true;
                     break;
                 }
-                const uint32_t a0 = sbase + A_RING + as * A_STAGE_BYTES + sts_off;
+                const uint32_t *xs = reinterpret_cast<const uint32_t *>(smem_tc + D_RING + ds * D_STAGE_BYTES + lds_off);
+                uint32_t xr[16];
 #pragma unroll
-                for (int kg = 0; kg < TC_KC / 8; kg++) {
-                    uint32_t uu[8][4];
+                for (int j = 0; j < 16; j++) xr[j] = biased(xs[j * TC_M], p);
+                mbar_arrive(&C.d_empty[ds]);
+                uint32_t w[4][8];     // [digit][row pair]
 #pragma unroll
-                    for (int j = 0; j < 8; j++) digits4(xr[kg * 8 + j], p, uu[j]);
+                for (int j = 0; j < 8; j++) {
+                    uint32_t d4[4];
+                    digit_pairs(xr[2 * j], xr[2 * j + 1], d4);
 #pragma unroll
-                    for (int l = 0; l < 4; l++)
-                        sts128(a0 + l * A_LIMB_BYTES + kg * 2048, digit_pair(uu[0][l], uu[1][l]),
-                               digit_pair(uu[2][l], uu[3][l]), digit_pair(uu[4][l], uu[5][l]),
-                               digit_pair(uu[6][l], uu[7][l]));
+                    for (int l = 0; l < 4; l++) w[l][j] = d4[l];
                 }
-                // make the generic-proxy stores visible to the tensor cores
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_arrive(&C.a_full[as]);
+                // buffer h held this parity's K-step of the previous stage
+                ok = G == 0 || mbar_wait_bounded(&C.a_empty[h], (G - 1) & 1, abort);
+                if (!__all_sync(0xffffffffu, ok)) {
+                    stop = true;
+                    break;
+                }
+                tc_fence_after();
 #pragma unroll
-                for (int j = 0; j < TC_KC; j++) xr[j] = xn[j];
+                for (int l = 0; l < 4; l++) tmem_st8(ta0 + 8 * l, w[l]);
+                tmem_wait_st();
+                tc_fence_before();
+                mbar_arrive(&C.a_full[h]);
             }
+            if (stop) break;
+            // this unit's share of the drain
+            const bool ok = mbar_wait_bounded(&C.acc_full, ui & 1, abort);
+            if (!__all_sync(0xffffffffu, ok)) break;
+            tc_fence_after();
+            drain_quarter(lane_addr, N, c0, L, z0, zc, u, m, out);
+            tc_fence_before();
+            mbar_arrive(&C.acc_empty);
         }
     } else {
-        // ----------------------------------------------------- epilogue
+        // -------------------------------------------------------- drain
         const int q4 = warp & 3;             // TMEM lane quarter of this warp
+        const int c0 = (2 + ((warp - 10) >> 2)) * 8;   // drain chunks 2, 6, ... or 3, 7, ...
         const int m = q4 * 32 + lane;
         const uint32_t lane_addr = tmem + ((uint32_t)(q4 * 32) << 16);
+        {
+            const uint32_t zero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (int n0 = c0; n0 < N; n0 += 32)
+#pragma unroll
+                for (int d = 0; d < 7; d++) tmem_st8(lane_addr + d * N + n0, zero8);
+            tmem_wait_st();
+            tc_fence_before();
+            mbar_arrive(&C.acc_empty);
+        }
         uint32_t ui = 0;
-        for (uint64_t u = blockIdx.x; u < units; u += gridDim.x, ui++) {
+        for (uint64_t v = blockIdx.x; v < units; v += gridDim.x, ui++) {
             // tcgen05.ld is warp-collective: the warp leaves together
             const bool ok = mbar_wait_bounded(&C.acc_full, ui & 1, abort);
             if (!__all_sync(0xffffffffu, ok)) break;
             tc_fence_after();
-            const int cbi = (int)(u % L.ncb);
-            const int z = (int)((u / L.ncb) % D);
-            const int prime = (int)(u / ((uint64_t)L.ncb * D));
-            const uint32_t p = prime ? QP1 : QP0;
-            const uint64_t mu = ~0ull / p;
-            const uint64_t off = ((1ull << 54) / p + 1) * p;
-            uint32_t w[7];
-            w[0] = 1;
-#pragma unroll
-            for (int d = 1; d < 7; d++) w[d] = (uint32_t)(((uint64_t)w[d - 1] << 7) % p);
-            const uint64_t mg = (uint64_t)cbi * TC_M + m;
-            for (int n0 = 0; n0 < N; n0 += 16) {
-                uint32_t v[7][16];
-#pragma unroll
-                for (int d = 0; d < 7; d++) tmem_ld16(lane_addr + d * N + n0, v[d]);
-                tmem_wait_ld();
-#pragma unroll
-                for (int c = 0; c < 16; c++) {
-                    const int n = n0 + c, b = n >> 1, k = n & 1;
-                    int64_t s = 0;
-#pragma unroll
-                    for (int d = 0; d < 7; d++) s += (int64_t)__float2int_rn(__uint_as_float(v[d][c])) * w[d];
-                    if (b < nq)
-                        C.acc[b][((mg * 2 + k) * 2 + prime) * D + z] =
-                            mod_u64_barrett((uint64_t)(s + (int64_t)off), p, mu);
-                }
-            }
+            drain_quarter(lane_addr, N, c0, L, z0, zc, chunk_unit(L, z0, zc, v), m, out);
             tc_fence_before();
             mbar_arrive(&C.acc_empty);
         }
@@ -396,14 +534,46 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_db_mul_tc(const uint32_t *__r
     }
 }
 
+// ------------------------------------------------------------ transpose
+// Chunk output [prime][z - z0][n][combo] -> each query's accumulator planes
+// [combo][ct row][prime][z].  Tile: 8 n x 32 slots x 32 combos through
+// shared memory; 128-byte reads and writes.
+__global__ void __launch_bounds__(256) k_tc_transpose(const uint32_t *__restrict__ in, const QDesc *__restrict__ qd,
+                                                      int nq, int N, int combos, int z0, int zc) {
+    __shared__ uint32_t tile[8][32][33];
+    const int mb = blockIdx.x * 32;
+    const int zb = blockIdx.y * 32;
+    const int prime = blockIdx.z / (N / 8), nb = (blockIdx.z % (N / 8)) * 8;
+    for (int i = threadIdx.x; i < 8 * 32 * 32; i += 256) {
+        const int m = i & 31, z = (i >> 5) & 31, n = i >> 10;
+        tile[n][z][m] = in[(((uint64_t)prime * zc + zb + z) * N + nb + n) * combos + mb + m];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 8 * 32 * 32; i += 256) {
+        const int z = i & 31, m = (i >> 5) & 31, n = i >> 10;
+        const int b = (nb + n) >> 1, k = (nb + n) & 1;
+        if (b < nq) qd[b].acc[(((uint64_t)(mb + m) * 2 + k) * 2 + prime) * D + z0 + zb + z] = tile[n][z][m];
+    }
+}
+
 bool db_mul_tc_supported(const DbLayout &L) {
     return L.cb == TC_M && L.rows % TC_KC == 0 && L.rows >= TC_KC && L.rows <= 512;
 }
 
 uint64_t tc_limb_bytes(const DbLayout &L) { return 2ull * D * L.rows * TC_MAX_N * 8; }
 
+// Slots per launch: the chunk output (2 * zc * combos * 64 * 4 bytes) stays
+// within 512 MiB.
+static int tc_chunk(const DbLayout &L) {
+    int zc = D;
+    while (zc > 32 && 2ull * zc * L.combos * TC_MAX_N * 4 > (512ull << 20)) zc >>= 1;
+    return zc;
+}
+
+uint64_t tc_out_bytes(const DbLayout &L) { return 2ull * tc_chunk(L) * L.combos * TC_MAX_N * 4; }
+
 cudaError_t launch_db_mul_tc(const uint32_t *db, const DbLayout &L, const QDesc *qd, int nq, uint8_t *limbs,
-                             int *err, cudaStream_t st) {
+                             uint32_t *out, int *err, cudaStream_t st) {
     if (!db_mul_tc_supported(L) || nq < 1 || nq > TC_MAX_Q) return cudaErrorInvalidValue;
     const int N = ((2 * nq + 15) / 16) * 16;
     const uint64_t total = (uint64_t)N * D * (L.rows / 8);
@@ -415,10 +585,19 @@ cudaError_t launch_db_mul_tc(const uint32_t *db, const DbLayout &L, const QDesc 
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute(k_db_mul_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
     if (e != cudaSuccess) return e;
-    const uint64_t units = L.units();
-    const int grid = (int)(units < (uint64_t)sms ? units : (uint64_t)sms);
-    k_db_mul_tc<<<grid, TC_THREADS, TC_SMEM, st>>>(db, L, qd, nq, N, limbs, err);
-    return cudaGetLastError();
+    const int zc = tc_chunk(L);
+    for (int z0 = 0; z0 < D; z0 += zc) {
+        const uint64_t units = 2ull * zc * L.ncb;
+        const int grid = (int)(units < (uint64_t)sms ? units : (uint64_t)sms);
+        k_db_mul_tc<<<grid, TC_THREADS, TC_SMEM, st>>>(db, L, nq, N, z0, zc, limbs, out, err);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        dim3 tg(L.combos / 32, zc / 32, 2 * (N / 8));
+        k_tc_transpose<<<tg, 256, 0, st>>>(out, qd, nq, N, L.combos, z0, zc);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 }  // namespace sp

@@ -102,14 +102,17 @@ cudaError_t launch_db_mul(const uint32_t *db, const DbLayout &L, const QDesc *qd
 bool db_mul_batch_supported(const DbLayout &L);
 cudaError_t launch_db_mul_batch(const uint32_t *db, const DbLayout &L, const QDesc *qd, int nq, cudaStream_t st);
 
-// Tensor-core variant (tcgen05, exact fp16 limb products): the selectors of
-// up to TC_MAX_Q queries are first split into limb tiles in `limbs`
-// (tc_limb_bytes(L) bytes), then each unit of the image is multiplied by
-// them with fp32 accumulation in tensor memory.
+// Tensor-core variant (tcgen05, exact fp16 digit products): the selectors of
+// up to TC_MAX_Q queries are first split into digit tiles in `limbs`
+// (tc_limb_bytes(L) bytes); each unit of the image is then multiplied by them
+// with fp32 accumulation in tensor memory, in launches over chunks of slots
+// whose results pass through `out` (tc_out_bytes(L) bytes) on their way to
+// the queries' accumulator planes.
 constexpr int TC_MAX_Q = 32;
 bool db_mul_tc_supported(const DbLayout &L);
 uint64_t tc_limb_bytes(const DbLayout &L);
+uint64_t tc_out_bytes(const DbLayout &L);
 cudaError_t launch_db_mul_tc(const uint32_t *db, const DbLayout &L, const QDesc *qd, int nq, uint8_t *limbs,
-                             int *err, cudaStream_t st);
+                             uint32_t *out, int *err, cudaStream_t st);
 
 }  // namespace sp

@@ -1,11 +1,14 @@
 """Small, bounded GPU cases for profiling one kernel under ncu.
 
     python -m spiralpir.profile_case db_mul --nu1 9 --nu2 4 --iters 3
+    python -m spiralpir.profile_case db_mul_batch --nu1 9 --nu2 5 --nq 32 --variant 3
     python -m spiralpir.profile_case answer --nu1 9 --nu2 8 --iters 2
 
 db_mul: one database of the given shape (random records) and random
 selectors; runs the first-dimension multiply `iters` times through
-sp_db_mul.  answer: a real client's queries answered `iters` times at the
+sp_db_mul.  db_mul_batch: the same for `nq` selector sets in one launch
+with multiply variant `variant` (1 per-query, 2 batched integer, 3 tensor
+core) through sp_db_mul_batch.  answer: a real client's queries answered `iters` times at the
 given shape (expansion, conversion, multiply, fold, pack kernels).
 Prints the device bytes held so that a capture stays small.
 """
@@ -22,23 +25,31 @@ from .lib import SpiralGPU
 
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["db_mul", "answer"])
+    ap.add_argument("case", choices=["db_mul", "db_mul_batch", "answer"])
     ap.add_argument("--nu1", type=int, default=9)
     ap.add_argument("--nu2", type=int, default=4)
     ap.add_argument("--iters", type=int, default=3)
+    ap.add_argument("--nq", type=int, default=32)
+    ap.add_argument("--variant", type=int, default=3)
     a = ap.parse_args()
     p = P.PARAMS
     sh = P.DbShape(a.nu1, a.nu2)
     recs = C.random_records(sh, p, seed=1)
     with SpiralGPU(p) as gpu:
         gpu.load_db(1, recs, sh.nu1, sh.nu2)
-        if a.case == "db_mul":
+        if a.case in ("db_mul", "db_mul_batch"):
             rng = np.random.default_rng(2)
             sel = np.empty((sh.rows, 2, 2, P.D), dtype=np.uint64)
             sel[:, :, 0] = rng.integers(0, P.Q1, size=(sh.rows, 2, P.D))
             sel[:, :, 1] = rng.integers(0, P.Q2, size=(sh.rows, 2, P.D))
-            for _ in range(a.iters):
-                gpu.db_mul(1, sel, p.T, sh.nu2)
+            if a.case == "db_mul":
+                for _ in range(a.iters):
+                    gpu.db_mul(1, sel, p.T, sh.nu2)
+            else:
+                sels = np.ascontiguousarray(np.broadcast_to(sel, (a.nq,) + sel.shape))
+                gpu.set_db_mul_variant(a.variant)
+                for _ in range(a.iters):
+                    gpu.db_mul_batch(1, sels, p.T, sh.nu2)
         else:
             cl = C.Client(p, seed=3)
             gpu.set_client_keys(1, cl.public_keys(sh.nu1, sh.nu2))

@@ -139,8 +139,9 @@ int sp_time_staged(sp_ctx *ctx, int32_t count, int32_t iters, double *ms_per_run
  * database and batch size, keep the fastest), 1 = per-query streaming kernel
  * (TMA-fed, HBM-bound), 2 = batched integer kernel (each residue read once per
  * 8 queries), 3 = tensor-core kernel (exact fp16 digit products, up to 32
- * queries per pass; needs 128 combos per block and at most 512 rows, and a
- * workspace of rows * 2 MiB per pipeline lane).  A forced variant that does
+ * queries per pass over the image; needs 128 combos per block and at most
+ * 512 rows, and a workspace of rows * 2 MiB + up to 512 MiB per pipeline
+ * lane).  A forced variant that does
  * not apply falls back to the autotuner.  sp_time_db_mul times the forced
  * variant (1 when none is forced).  The result is identical. */
 int sp_set_db_mul_variant(sp_ctx *ctx, int32_t variant);
