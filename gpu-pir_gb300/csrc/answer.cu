@@ -12,11 +12,11 @@ namespace {
 
 constexpr int THREADS = 256;
 // shared memory: 4 twiddle tables + per group 2 transpose buffers
-constexpr int SMEM_WORDS = 4 * D + 2 * 2 * D;
+constexpr int SMEM_WORDS = TW_WORDS + 2 * 2 * D;
 constexpr int SMEM_BYTES = SMEM_WORDS * 4;
 
 struct Ctx {
-    uint32_t *tw;    // 4 tables
+    const uint32_t *tw;   // 4 tables (TW_WORDS words)
     uint32_t *buf;   // this group's two transpose buffers
     uint32_t *bufs;  // both groups' buffers (exchange area, 4*D words)
     Prime c;
@@ -30,15 +30,15 @@ __device__ __forceinline__ Ctx setup(uint32_t *smem, const TwiddleSet *tws) {
     x.t = threadIdx.x & (GROUP - 1);
     x.c = prime_of(x.g);
     x.tw = smem;
-    x.bufs = smem + 4 * D;
+    x.bufs = smem + TW_WORDS;
     x.buf = x.bufs + x.g * 2 * D;
     x.bar = 1 + x.g;
     __syncthreads();
     return x;
 }
 
-__device__ __forceinline__ const uint32_t *tw_fwd(const Ctx &x) { return x.tw + x.g * D; }
-__device__ __forceinline__ const uint32_t *tw_inv(const Ctx &x) { return x.tw + (2 + x.g) * D; }
+__device__ __forceinline__ const uint2 *tw_fwd(const Ctx &x) { return tw_of(x.tw, x.g); }
+__device__ __forceinline__ const uint2 *tw_inv(const Ctx &x) { return tw_of(x.tw, 2 + x.g); }
 
 // Both groups hold unscaled INTT outputs (layout A, < 2p) of the same
 // polynomial mod their prime; returns the raw coefficients of this thread's
@@ -155,9 +155,9 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_expand_round(const QDesc *
     load_twiddles(smem, tws);
     const int gi = threadIdx.x >> 7, g = gi & 1, sub = gi >> 1, t = threadIdx.x & (GROUP - 1), bar = 1 + gi;
     const Prime c = prime_of(g);
-    uint32_t *bufs = smem + 4 * D;
+    uint32_t *bufs = smem + TW_WORDS;
     uint32_t *buf = bufs + gi * 2 * D;
-    const uint32_t *twf = smem + g * D, *twi = smem + (2 + g) * D;
+    const uint2 *twf = tw_of(smem, g), *twi = tw_of(smem, 2 + g);
     __syncthreads();
     const int half = 1 << r;
     const bool upper = i >= half;
@@ -258,7 +258,7 @@ cudaError_t launch_expand_round(const QDesc *qd, int nq, int r, int max_out, con
                                 const TwiddleSet *tw, const uint32_t *neg1, cudaStream_t st) {
     const bool wide = (uint64_t)max_out * nq < 2ull * sm_count();
     if (wide) {
-        const int smem = (4 * D + 4 * 2 * D) * 4 + D * 8;
+        const int smem = (TW_WORDS + 4 * 2 * D) * 4 + D * 8;
         cudaError_t e = cudaFuncSetAttribute(k_expand_round<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
         k_expand_round<2><<<dim3(max_out, nq), 512, smem, st>>>(qd, r, sp, tw, neg1);
@@ -430,9 +430,9 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_fold_level(const QDesc *__
     load_twiddles(smem, tws);
     const int gi = threadIdx.x >> 7, g = gi & 1, sub = gi >> 1, t = threadIdx.x & (GROUP - 1), bar = 1 + gi;
     const Prime c = prime_of(g);
-    uint32_t *bufs = smem + 4 * D;           // [group][2][D]
+    uint32_t *bufs = smem + TW_WORDS;           // [group][2][D]
     uint32_t *buf = bufs + gi * 2 * D;
-    const uint32_t *twf = smem + g * D, *twi = smem + (2 + g) * D;
+    const uint2 *twf = tw_of(smem, g), *twi = tw_of(smem, 2 + g);
     __syncthreads();
     const int cols = 1 << Q.nu2;
     uint64_t *base = Q.raw + (size_t)inst * cols * 2 * D;
@@ -513,7 +513,7 @@ cudaError_t launch_fold_level(const QDesc *qd, int nq, int level, int max_items,
                               const TwiddleSet *tw, cudaStream_t st) {
     const bool wide = (uint64_t)max_items * nq < 2ull * sm_count();
     if (wide) {
-        const int smem = (4 * D + 4 * 2 * D) * 4;
+        const int smem = (TW_WORDS + 4 * 2 * D) * 4;
         cudaError_t e = cudaFuncSetAttribute(k_fold_level<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
         k_fold_level<2><<<dim3(max_items, nq), 512, smem, st>>>(qd, level, sp, tw);

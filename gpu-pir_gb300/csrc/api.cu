@@ -103,6 +103,10 @@ struct Lane {
     int staged = 0;
     bool busy = false;                  // serving: a batch is in flight
     std::vector<uint64_t> tickets;      // serving: tickets of that batch, slot order
+    // instantiated pipeline graphs, keyed by the batch plan (see run_pipeline),
+    // and how often each plan has run
+    std::map<std::vector<int64_t>, cudaGraphExec_t> graphs;
+    std::map<std::vector<int64_t>, int> plan_runs;
 };
 
 struct Pending {
@@ -143,6 +147,7 @@ struct sp_ctx {
     // 3 = tensor-core kernel
     std::map<std::pair<int, int>, int> mul_choice;
     int mul_force = 0;          // 0 = autotune, 1..3 = force a variant
+    bool use_graphs = true;     // replay the answer pipeline as CUDA graphs
     // serving (continuous batching)
     std::vector<Lane *> lanes;
     std::thread worker;
@@ -290,7 +295,16 @@ int lane_init(sp_ctx *c, Lane &L, int cap) {
     return SP_OK;
 }
 
+// Graph instances bake in kernel arguments (descriptor array, database
+// images, multiply workspace): drop them when one of those moves.
+void clear_graphs(Lane &L) {
+    for (auto &kv : L.graphs) cudaGraphExecDestroy(kv.second);
+    L.graphs.clear();
+    L.plan_runs.clear();
+}
+
 void lane_free(sp_ctx *c, Lane &L) {
+    clear_graphs(L);
     if (L.st) cudaStreamSynchronize(L.st);
     for (auto &sl : L.slots) release(c, sl.base, sl.bytes);
     L.slots.clear();
@@ -313,6 +327,11 @@ void lane_free(sp_ctx *c, Lane &L) {
     if (L.done) cudaEventDestroy(L.done);
     if (L.st) cudaStreamDestroy(L.st);
     L.st = nullptr;
+}
+
+void clear_all_graphs(sp_ctx *c) {
+    clear_graphs(c->main);
+    for (Lane *l : c->lanes) clear_graphs(*l);
 }
 
 // Wait for the GPU work of every lane (before freeing keys or databases).
@@ -357,6 +376,7 @@ bool ensure_limbs(sp_ctx *c, Lane &L, const DbLayout &dl) {
     if (L.limb_bytes >= need_l && L.tc_out_bytes >= need_o) return true;
     if (L.limbs || L.tc_out) {
         if (cudaStreamSynchronize(L.st) != cudaSuccess) return false;
+        clear_graphs(L);
     }
     if (L.limb_bytes < need_l) {
         release(c, L.limbs, L.limb_bytes);
@@ -450,7 +470,16 @@ int choose_mul_variant(sp_ctx *c, Lane &L, int db_id, const Db &db, const QDesc 
 }
 
 // Run the answer pipeline for queries in slots [0, nq) (descriptors already
-// in c->h_qd / c->d_qd, queries in slot.query32).  Records stage events.
+// in L.h_qd / L.d_qd, queries in slot.query32).  Records stage events.
+//
+// The launches depend only on the batch plan: query count, the largest
+// expansion depth / fold depth / conversion size, and per run of slots on one
+// database its id, length and multiply variant.  The plan is the key of an
+// instantiated CUDA graph of the whole pipeline (stage events included),
+// captured the second time the plan runs (a capture costs more than one
+// replay saves) and replayed afterwards; per-query inputs reach the kernels
+// through the descriptor array, which is uploaded before each run.  A lane
+// keeps at most 256 graphs; further plans run as plain launches.
 int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot) {
     cudaStream_t st = L.st;
     const StageParams &sp = c->sp;
@@ -460,46 +489,84 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot)
         max_nu2 = std::max(max_nu2, L.h_qd[i].nu2);
         max_items = std::max(max_items, L.h_qd[i].nu2 * sp.t_gsw);
     }
-    uint64_t launches = 0;
-    CU(cudaEventRecord(L.ev[0], st));
-    for (int r = 0; r < max_g; r++) {
-        CU(launch_expand_round(L.d_qd, nq, r, 2 << r, sp, c->d_tw, c->d_neg1, st));
-        launches++;
-    }
-    CU(cudaEventRecord(L.ev[1], st));
-    CU(launch_regev_to_gsw(L.d_qd, nq, max_items, sp, c->d_tw, st));
-    launches++;
-    CU(cudaEventRecord(L.ev[2], st));
-    // first-dimension multiply: consecutive slots of the same database share a launch
-    uint64_t mul_bytes = 0, mul_calls = 0;
+    // first-dimension multiply: consecutive slots of the same database share
+    // a launch; variants are chosen (and autotuned) before any capture
+    struct Group {
+        int db_id, begin, count, variant;
+    };
+    std::vector<Group> groups;
+    std::vector<int64_t> key = {nq, max_g, max_nu2, max_items};
+    uint64_t mul_bytes = 0;
     for (int i = 0; i < nq;) {
         int j = i;
         while (j < nq && db_of_slot[j] == db_of_slot[i]) j++;
         const Db &db = c->dbs.at(db_of_slot[i]);
         int variant = 1;
         TRY(choose_mul_variant(c, L, db_of_slot[i], db, L.d_qd + i, j - i, &variant));
-        CU(launch_mul_variant(L, db, L.d_qd + i, j - i, variant));
-        c->stats.db_mul_by_variant[variant - 1]++;
-        launches++;
-        mul_calls++;
+        groups.push_back({db_of_slot[i], i, j - i, variant});
+        key.insert(key.end(), {db_of_slot[i], j - i, variant});
         mul_bytes += db.L.words * 8 + (uint64_t)(j - i) * ((uint64_t)db.L.rows * D * 16 +
                                                           (uint64_t)db.L.T * db.L.cols * 4 * D * 4);
         i = j;
     }
-    CU(cudaEventRecord(L.ev[3], st));
-    CU(launch_acc_to_raw(L.d_qd, nq, sp.T * (2 << max_nu2), sp, c->d_tw, st));
-    launches++;
-    for (int lvl = 0; lvl < max_nu2; lvl++) {
-        CU(launch_fold_level(L.d_qd, nq, lvl, sp.T << (max_nu2 - 1 - lvl), sp, c->d_tw, st));
-        launches++;
+    // stage events are recorded as external event nodes so that a replayed
+    // graph records them too
+    auto enqueue = [&](bool capturing) -> cudaError_t {
+        const unsigned ev_flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+        cudaError_t e = cudaEventRecordWithFlags(L.ev[0], st, ev_flags);
+        for (int r = 0; r < max_g && !e; r++) e = launch_expand_round(L.d_qd, nq, r, 2 << r, sp, c->d_tw, c->d_neg1, st);
+        if (!e) e = cudaEventRecordWithFlags(L.ev[1], st, ev_flags);
+        if (!e) e = launch_regev_to_gsw(L.d_qd, nq, max_items, sp, c->d_tw, st);
+        if (!e) e = cudaEventRecordWithFlags(L.ev[2], st, ev_flags);
+        for (const Group &gr : groups) {
+            if (e) break;
+            e = launch_mul_variant(L, c->dbs.at(gr.db_id), L.d_qd + gr.begin, gr.count, gr.variant);
+        }
+        if (!e) e = cudaEventRecordWithFlags(L.ev[3], st, ev_flags);
+        if (!e) e = launch_acc_to_raw(L.d_qd, nq, sp.T * (2 << max_nu2), sp, c->d_tw, st);
+        for (int lvl = 0; lvl < max_nu2 && !e; lvl++)
+            e = launch_fold_level(L.d_qd, nq, lvl, sp.T << (max_nu2 - 1 - lvl), sp, c->d_tw, st);
+        if (!e) e = cudaEventRecordWithFlags(L.ev[4], st, ev_flags);
+        if (!e) e = launch_pack(L.d_qd, nq, sp, c->d_tw, st);
+        if (!e) e = launch_bitpack(L.d_qd, nq, sp, response_bytes(sp), st);
+        if (!e) e = cudaEventRecordWithFlags(L.ev[5], st, ev_flags);
+        return e;
+    };
+    auto it = L.graphs.find(key);
+    bool replay = c->use_graphs && it != L.graphs.end();
+    if (c->use_graphs && !replay && L.graphs.size() < 256) {
+        if (L.plan_runs.size() > 4096) L.plan_runs.clear();
+        replay = ++L.plan_runs[key] >= 2;
     }
-    CU(cudaEventRecord(L.ev[4], st));
-    CU(launch_pack(L.d_qd, nq, sp, c->d_tw, st));
-    CU(launch_bitpack(L.d_qd, nq, sp, response_bytes(sp), st));
-    launches += 2;
-    CU(cudaEventRecord(L.ev[5], st));
+    if (replay) {
+        if (it == L.graphs.end()) {
+            cudaGraph_t graph = nullptr;
+            CU(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+            const cudaError_t e = enqueue(true);
+            const cudaError_t e2 = cudaStreamEndCapture(st, &graph);
+            if (e != cudaSuccess || e2 != cudaSuccess) {
+                if (graph) cudaGraphDestroy(graph);
+                cudaGetLastError();
+                return fail(SP_ERR_CUDA, std::string("pipeline capture: ") +
+                                             cudaGetErrorString(e != cudaSuccess ? e : e2));
+            }
+            cudaGraphExec_t exec = nullptr;
+            const cudaError_t e3 = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e3 != cudaSuccess) return fail(SP_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e3));
+            it = L.graphs.emplace(key, exec).first;
+        }
+        CU(cudaGraphLaunch(it->second, st));
+    } else {
+        CU(enqueue(false));
+    }
+    uint64_t launches = (uint64_t)max_g + 1 + 1 + (uint64_t)max_nu2 + 2;
+    for (const Group &gr : groups) {
+        c->stats.db_mul_by_variant[gr.variant - 1]++;
+        launches += gr.variant == 3 ? 3 * (uint64_t)((gr.count + TC_MAX_Q - 1) / TC_MAX_Q) : 1;
+    }
     c->stats.launches += launches;
-    c->stats.db_mul_calls += mul_calls;
+    c->stats.db_mul_calls += groups.size();
     c->stats.db_mul_bytes += mul_bytes;
     c->stats.answers += nq;
     return SP_OK;
@@ -660,6 +727,7 @@ static int db_alloc(sp_ctx *c, int db_id, int nu1, int nu2, Db &db) {
     TRY(db_check_shape(c, nu1, nu2));
     if (c->dbs.count(db_id)) {
         TRY(sync_all(c));
+        clear_all_graphs(c);
         release(c, c->dbs[db_id].d, c->dbs[db_id].bytes);
         c->dbs.erase(db_id);
     }
@@ -741,6 +809,7 @@ int sp_db_unload(sp_ctx *c, int32_t db_id) {
     auto it = c->dbs.find(db_id);
     if (it == c->dbs.end()) return fail(SP_ERR_NOT_FOUND, "unknown database id");
     TRY(sync_all(c));
+    clear_all_graphs(c);
     release(c, it->second.d, it->second.bytes);
     c->dbs.erase(it);
     return SP_OK;
@@ -977,6 +1046,13 @@ int sp_set_db_mul_variant(sp_ctx *c, int32_t variant) {
     if (variant < 0 || variant > 3) return fail(SP_ERR_INVALID, "variant must be 0 (auto), 1, 2 or 3");
     std::lock_guard<std::mutex> lk(c->mu);
     c->mul_force = variant;
+    return SP_OK;
+}
+
+int sp_set_graphs(sp_ctx *c, int32_t on) {
+    if (!c) return fail(SP_ERR_INVALID, "NULL context");
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->use_graphs = on != 0;
     return SP_OK;
 }
 

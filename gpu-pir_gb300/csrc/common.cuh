@@ -142,27 +142,40 @@ __host__ __device__ __forceinline__ constexpr int swz(int e) {
 }
 
 // --------------------------------------------------------- twiddle tables
-// Per (prime, direction): 2048 u32 in Montgomery form.  Entry m+i holds
-// psi^(+-brev11(m+i)) (block i of the stage with m blocks) for m < 256; the
-// last three stages (m = 256, 512, 1024; c = m/128 twiddles per thread) are
-// restrided so that entry m + k*128 + t holds twiddle m + c*t + k.
+// Per (prime, direction): 2048 pairs (w, floor(w * 2^32 / p)) with w
+// canonical, for Shoup multiplication.  Entry m+i holds psi^(+-brev11(m+i))
+// (block i of the stage with m blocks) for m < 256; the last three stages
+// (m = 256, 512, 1024; c = m/128 twiddles per thread) are restrided so that
+// entry m + k*128 + t holds twiddle m + c*t + k.
 struct TwiddleSet {
-    uint32_t t[4][D];   // [fwd q1, fwd q2, inv q1, inv q2]
+    uint2 t[4][D];   // [fwd q1, fwd q2, inv q1, inv q2]
 };
+constexpr int TW_WORDS = 8 * D;   // u32 words of a TwiddleSet in shared memory
+
+// Table k (0, 1 forward; 2, 3 inverse) of a TwiddleSet copied to shared memory.
+__device__ __forceinline__ const uint2 *tw_of(const uint32_t *smem_tw, int k) {
+    return reinterpret_cast<const uint2 *>(smem_tw) + k * D;
+}
+
+// y * w mod p in [0, 2p) for any y < 2^32 (Shoup): wq = floor(w * 2^32 / p).
+__device__ __forceinline__ uint32_t shoup_mul(uint32_t y, uint32_t w, uint32_t wq, uint32_t p) {
+    const uint32_t q = __umulhi(y, wq);
+    return y * w - q * p;
+}
 
 // -------------------------------------------------------- NTT butterflies
-__device__ __forceinline__ void ct_bfly(uint32_t &x, uint32_t &y, uint32_t w, uint32_t p, uint32_t pinv) {
+__device__ __forceinline__ void ct_bfly(uint32_t &x, uint32_t &y, uint2 w, uint32_t p) {
     uint32_t xr = min(x, x - 2 * p);
-    uint32_t t = mont_mul(y, w, p, pinv);
+    uint32_t t = shoup_mul(y, w.x, w.y, p);
     x = xr + t;
     y = xr - t + 2 * p;
 }
 
-__device__ __forceinline__ void gs_bfly(uint32_t &x, uint32_t &y, uint32_t w, uint32_t p, uint32_t pinv) {
+__device__ __forceinline__ void gs_bfly(uint32_t &x, uint32_t &y, uint2 w, uint32_t p) {
     uint32_t s = x + y;
     uint32_t d = x - y + 2 * p;
     x = min(s, s - 2 * p);
-    y = mont_mul(d, w, p, pinv);
+    y = shoup_mul(d, w.x, w.y, p);
 }
 
 // Per-thread address bases of the three layouts (t: thread within group).
@@ -171,18 +184,18 @@ __device__ __forceinline__ int baseB(int t) { return swz(128 * (t >> 3) + (t & 7
 __device__ __forceinline__ int baseC(int t) { return swz(16 * t); }
 
 // Forward NTT of one plane.  v: layout A in (values < 4p), layout C out
-// (values < 4p).  tw: forward table of this prime (shared or global).
+// (values < 4p).  tw: forward table of this prime (shared memory).
 // buf: 2 x 2048 words of shared memory private to the group.
-__device__ __forceinline__ void ntt_fwd(uint32_t (&v)[VPT], const uint32_t *__restrict__ tw,
+__device__ __forceinline__ void ntt_fwd(uint32_t (&v)[VPT], const uint2 *__restrict__ tw,
                                         uint32_t *buf, const Prime &c, int t, int bar_id) {
-    const uint32_t p = c.p, pinv = c.pinv;
+    const uint32_t p = c.p;
     // phase A: h = 1024, 512, 256, 128  (pairs j, j + 8>>L)
 #pragma unroll
     for (int L = 0; L < 4; L++) {
         const int dj = 8 >> L;
 #pragma unroll
         for (int j = 0; j < VPT; j++)
-            if ((j & dj) == 0) ct_bfly(v[j], v[j + dj], tw[(1 << L) + j / (2 * dj)], p, pinv);
+            if ((j & dj) == 0) ct_bfly(v[j], v[j + dj], tw[(1 << L) + j / (2 * dj)], p);
     }
     // transpose A -> B
     {
@@ -204,7 +217,7 @@ __device__ __forceinline__ void ntt_fwd(uint32_t (&v)[VPT], const uint32_t *__re
 #pragma unroll
             for (int j = 0; j < VPT; j++)
                 if ((j & dj) == 0)
-                    ct_bfly(v[j], v[j + dj], tw[(1 << L) + (bb << (L - 4)) + (j >> (8 - L))], p, pinv);
+                    ct_bfly(v[j], v[j + dj], tw[(1 << L) + (bb << (L - 4)) + (j >> (8 - L))], p);
         }
     }
     // transpose B -> C
@@ -224,21 +237,21 @@ __device__ __forceinline__ void ntt_fwd(uint32_t (&v)[VPT], const uint32_t *__re
         const int dj = 4 >> (L - 8);
 #pragma unroll
         for (int j = 0; j < VPT; j++)
-            if ((j & dj) == 0) ct_bfly(v[j], v[j + dj], tw[(1 << L) + (j / (2 * dj)) * GROUP + t], p, pinv);
+            if ((j & dj) == 0) ct_bfly(v[j], v[j + dj], tw[(1 << L) + (j / (2 * dj)) * GROUP + t], p);
     }
 }
 
 // Inverse NTT of one plane (without the 2048^-1 scaling).  v: layout C in
 // (values < 2p), layout A out (values < 2p).
-__device__ __forceinline__ void ntt_inv(uint32_t (&v)[VPT], const uint32_t *__restrict__ tw,
+__device__ __forceinline__ void ntt_inv(uint32_t (&v)[VPT], const uint2 *__restrict__ tw,
                                         uint32_t *buf, const Prime &c, int t, int bar_id) {
-    const uint32_t p = c.p, pinv = c.pinv;
+    const uint32_t p = c.p;
 #pragma unroll
     for (int L = 10; L >= 8; L--) {
         const int dj = 4 >> (L - 8);
 #pragma unroll
         for (int j = 0; j < VPT; j++)
-            if ((j & dj) == 0) gs_bfly(v[j], v[j + dj], tw[(1 << L) + (j / (2 * dj)) * GROUP + t], p, pinv);
+            if ((j & dj) == 0) gs_bfly(v[j], v[j + dj], tw[(1 << L) + (j / (2 * dj)) * GROUP + t], p);
     }
     {
         uint32_t *b0 = buf;
@@ -258,7 +271,7 @@ __device__ __forceinline__ void ntt_inv(uint32_t (&v)[VPT], const uint32_t *__re
 #pragma unroll
             for (int j = 0; j < VPT; j++)
                 if ((j & dj) == 0)
-                    gs_bfly(v[j], v[j + dj], tw[(1 << L) + (bb << (L - 4)) + (j >> (8 - L))], p, pinv);
+                    gs_bfly(v[j], v[j + dj], tw[(1 << L) + (bb << (L - 4)) + (j >> (8 - L))], p);
         }
     }
     {
@@ -276,7 +289,7 @@ __device__ __forceinline__ void ntt_inv(uint32_t (&v)[VPT], const uint32_t *__re
         const int dj = 8 >> L;
 #pragma unroll
         for (int j = 0; j < VPT; j++)
-            if ((j & dj) == 0) gs_bfly(v[j], v[j + dj], tw[(1 << L) + j / (2 * dj)], p, pinv);
+            if ((j & dj) == 0) gs_bfly(v[j], v[j + dj], tw[(1 << L) + j / (2 * dj)], p);
     }
 }
 
@@ -284,7 +297,7 @@ __device__ __forceinline__ void ntt_inv(uint32_t (&v)[VPT], const uint32_t *__re
 __device__ __forceinline__ void load_twiddles(uint32_t *dst, const TwiddleSet *src) {
     const uint4 *s = reinterpret_cast<const uint4 *>(src);
     uint4 *d = reinterpret_cast<uint4 *>(dst);
-    for (int i = threadIdx.x; i < 4 * D / 4; i += blockDim.x) d[i] = __ldg(s + i);
+    for (int i = threadIdx.x; i < TW_WORDS / 4; i += blockDim.x) d[i] = __ldg(s + i);
 }
 
 // Slot permutation of the automorphism x -> x^tau in NTT form: the slot z

@@ -31,7 +31,7 @@ DbLayout make_db_layout(int T, int nu1, int nu2) {
 // ----------------------------------------------------------------- encode
 // One CTA per (record, t) polynomial: group g transforms residues mod q_g of
 // the recentred plaintext and writes its 32-bit half of the packed words.
-constexpr int ENC_SMEM_WORDS = 4 * D + 2 * 2 * D;
+constexpr int ENC_SMEM_WORDS = TW_WORDS + 2 * 2 * D;
 
 __global__ void __launch_bounds__(256) k_db_encode(const uint8_t *__restrict__ rec, uint64_t rec_begin,
                                                    uint64_t rec_count, int pt_bits, DbLayout L,
@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(256) k_db_encode(const uint8_t *__restrict__ r
     __syncthreads();
     const int g = threadIdx.x >> 7, t = threadIdx.x & (GROUP - 1);
     const Prime c = prime_of(g);
-    uint32_t *buf = smem + 4 * D + g * 2 * D;
+    uint32_t *buf = smem + TW_WORDS + g * 2 * D;
     const uint32_t pm = 1u << pt_bits;
     const uint64_t polys = rec_count * L.T;
     for (uint64_t i = blockIdx.x; i < polys; i += gridDim.x) {
@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(256) k_db_encode(const uint8_t *__restrict__ r
             uint32_t x = src[t + GROUP * j];
             v[j] = (x > pm / 2) ? c.p - (pm - x) : x;   // recentre to (-p/2, p/2]
         }
-        ntt_fwd(v, smem + g * D, buf, c, t, 1 + g);
+        ntt_fwd(v, tw_of(smem, g), buf, c, t, 1 + g);
 #pragma unroll
         for (int j = 0; j < VPT; j++) {
             const int z = VPT * t + j;

@@ -30,19 +30,27 @@ void build_twiddles_host(TwiddleSet *h) {
         const Prime c = prime_of(k);
         const uint64_t p = c.p;
         const uint64_t psi_inv = powmod_c(psi[k], 4095, p);
-        uint32_t f[D], iv[D];
+        uint32_t f[D], iv[D], fq[D], ivq[D], rf[D], riv[D], rfq[D], rivq[D];
         for (uint32_t i = 0; i < (uint32_t)D; i++) {
             uint32_t e = brev11(i);
-            f[i] = (uint32_t)(powmod_c(psi[k], e, p) * c.two32 % p);     // Montgomery form
-            iv[i] = (uint32_t)(powmod_c(psi_inv, e, p) * c.two32 % p);
+            f[i] = (uint32_t)powmod_c(psi[k], e, p);
+            iv[i] = (uint32_t)powmod_c(psi_inv, e, p);
+            fq[i] = (uint32_t)(((uint64_t)f[i] << 32) / p);      // Shoup companions
+            ivq[i] = (uint32_t)(((uint64_t)iv[i] << 32) / p);
         }
-        restride(f, h->t[k]);
-        restride(iv, h->t[2 + k]);
+        restride(f, rf);
+        restride(iv, riv);
+        restride(fq, rfq);
+        restride(ivq, rivq);
+        for (int i = 0; i < D; i++) {
+            h->t[k][i] = make_uint2(rf[i], rfq[i]);
+            h->t[2 + k][i] = make_uint2(riv[i], rivq[i]);
+        }
     }
 }
 
 // Shared memory of the NTT kernels: 4 twiddle tables + 2 groups x 2 buffers.
-constexpr int NTT_SMEM_WORDS = 4 * D + 2 * 2 * D;
+constexpr int NTT_SMEM_WORDS = TW_WORDS + 2 * 2 * D;
 
 __global__ void __launch_bounds__(256) k_to_ntt(const uint64_t *__restrict__ raw, uint32_t *__restrict__ out,
                                                 int count, const TwiddleSet *__restrict__ tws) {
@@ -51,13 +59,13 @@ __global__ void __launch_bounds__(256) k_to_ntt(const uint64_t *__restrict__ raw
     __syncthreads();
     const int g = threadIdx.x >> 7, t = threadIdx.x & (GROUP - 1);
     const Prime c = prime_of(g);
-    uint32_t *buf = smem + 4 * D + g * 2 * D;
+    uint32_t *buf = smem + TW_WORDS + g * 2 * D;
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
         uint32_t v[VPT];
         const uint64_t *src = raw + (size_t)i * D;
 #pragma unroll
         for (int j = 0; j < VPT; j++) v[j] = mod_u64(src[t + GROUP * j], c);
-        ntt_fwd(v, smem + g * D, buf, c, t, 1 + g);
+        ntt_fwd(v, tw_of(smem, g), buf, c, t, 1 + g);
 #pragma unroll
         for (int j = 0; j < VPT; j++) v[j] = canon4(v[j], c.p);
         st16(out + ((size_t)i * 2 + g) * D + VPT * t, v);
@@ -71,7 +79,7 @@ __global__ void __launch_bounds__(256) k_from_ntt(const uint32_t *__restrict__ i
     __syncthreads();
     const int g = threadIdx.x >> 7, t = threadIdx.x & (GROUP - 1);
     const Prime c = prime_of(g);
-    uint32_t *buf = smem + 4 * D + g * 2 * D;
+    uint32_t *buf = smem + TW_WORDS + g * 2 * D;
     // exchange area: reuse of the twiddle-free region is not possible (tables
     // are live), so it follows the group buffers.
     uint32_t *xch = smem + NTT_SMEM_WORDS;
@@ -80,7 +88,7 @@ __global__ void __launch_bounds__(256) k_from_ntt(const uint32_t *__restrict__ i
         ld16(v, in + ((size_t)i * 2 + g) * D + VPT * t);
 #pragma unroll
         for (int j = 0; j < VPT; j++) v[j] = reduce2(v[j], 2 * c.p) ;
-        ntt_inv(v, smem + (2 + g) * D, buf, c, t, 1 + g);
+        ntt_inv(v, tw_of(smem, 2 + g), buf, c, t, 1 + g);
 #pragma unroll
         for (int j = 0; j < VPT; j++) xch[g * D + t + GROUP * j] = v[j];
         __syncthreads();
@@ -101,21 +109,21 @@ __global__ void __launch_bounds__(256) k_ntt_planes(uint32_t *__restrict__ a, in
     __syncthreads();
     const int g = threadIdx.x >> 7, t = threadIdx.x & (GROUP - 1);
     const Prime c = prime_of(g);
-    uint32_t *buf = smem + 4 * D + g * 2 * D;
+    uint32_t *buf = smem + TW_WORDS + g * 2 * D;
     for (int i = blockIdx.x; i < count; i += gridDim.x) {
         uint32_t *pl = a + ((size_t)i * 2 + g) * D;
         uint32_t v[VPT];
         if (!inverse) {
 #pragma unroll
             for (int j = 0; j < VPT; j++) v[j] = pl[t + GROUP * j];
-            ntt_fwd(v, smem + g * D, buf, c, t, 1 + g);
+            ntt_fwd(v, tw_of(smem, g), buf, c, t, 1 + g);
 #pragma unroll
             for (int j = 0; j < VPT; j++) v[j] = canon4(v[j], c.p);
             group_sync(1 + g);  // all reads of this plane done before writes
             st16(pl + VPT * t, v);
         } else {
             ld16(v, pl + VPT * t);
-            ntt_inv(v, smem + (2 + g) * D, buf, c, t, 1 + g);
+            ntt_inv(v, tw_of(smem, 2 + g), buf, c, t, 1 + g);
 #pragma unroll
             for (int j = 0; j < VPT; j++) {
                 uint32_t x = mont_mul(v[j], c.ninv_m, c.p, c.pinv);

@@ -94,6 +94,7 @@ _SIGS = {
     "sp_gsw_neg": [_P, _P, _I, _P],
     "sp_db_mul": [_P, _I, _P, _P],
     "sp_db_mul_batch": [_P, _I, _I, _P, _P],
+    "sp_set_graphs": [_P, _I],
     "sp_fold": [_P, _P, _P, _I, _I, _P],
     "sp_fold_noalloc": [_P, _P, _P, _I, _I, _P],
     "sp_pack": [_P, _I, _P, _P, _U64],
@@ -232,6 +233,11 @@ class SpiralGPU:
         """0 = autotune, 1 = per-query streaming multiply, 2 = batched integer
         multiply, 3 = tensor-core multiply."""
         _check(self.lib.sp_set_db_mul_variant(self.h, variant))
+
+    def set_graphs(self, on: bool) -> None:
+        """Replay the answer pipeline as CUDA graphs (default) or launch its
+        kernels one by one."""
+        _check(self.lib.sp_set_graphs(self.h, 1 if on else 0))
 
     def stats(self) -> dict:
         s = SpStats()

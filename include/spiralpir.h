@@ -145,6 +145,12 @@ int sp_time_staged(sp_ctx *ctx, int32_t count, int32_t iters, double *ms_per_run
  * not apply falls back to the autotuner.  sp_time_db_mul times the forced
  * variant (1 when none is forced).  The result is identical. */
 int sp_set_db_mul_variant(sp_ctx *ctx, int32_t variant);
+/* Answer pipelines run as CUDA graphs (default on): the launches of a batch
+ * plan (query count, expansion and fold depths, and the database, length and
+ * multiply variant of each run of slots) are captured once per pipeline lane
+ * and replayed.  Off: the same launches are issued one by one.  Reloading a
+ * database drops the captured graphs.  No counterpart in the reference. */
+int sp_set_graphs(sp_ctx *ctx, int32_t on);
 /* Serving loop (continuous batching).  sp_serve_start starts a worker thread
  * with `lanes` pipeline lanes (each its own stream and max_batch workspace
  * slots).  sp_submit copies the request's query and returns a ticket; the

@@ -60,6 +60,41 @@ def test_batch_variants_match_alone(world, variant):
         gpu.set_db_mul_variant(0)
 
 
+def test_graph_replay_matches_direct_launches(world):
+    """The same batch plan run with plain launches, then captured (second
+    run) and replayed: every response is identical to the query alone."""
+    gpu, _, reqs, alone = world
+    batch = [(c, d, q) for c, d, q, _, _ in reqs[:8]]
+    try:
+        gpu.set_graphs(False)
+        direct = gpu.answer_batch(batch)
+        gpu.set_graphs(True)
+        runs = [gpu.answer_batch(batch) for _ in range(3)]
+    finally:
+        gpu.set_graphs(True)
+    for got in [direct] + runs:
+        for x, y in zip(got, alone[:8]):
+            assert np.array_equal(x, y)
+
+
+def test_graphs_dropped_when_database_reloaded():
+    """A captured plan refers to the database image; reloading the database
+    under the same id must not replay stale pointers."""
+    p = P.PARAMS
+    sh = P.SHAPE_8MIB
+    cl = C.Client(p, seed=81)
+    with SpiralGPU(p, max_batch=4) as gpu:
+        gpu.set_client_keys(1, cl.public_keys(sh.nu1, sh.nu2))
+        for seed in (82, 83):
+            recs = C.random_records(sh, p, seed=seed)
+            gpu.load_db(1, recs, sh.nu1, sh.nu2)
+            idx = [3, 500, 1000, 7]
+            qs = [(1, 1, cl.query(sh, i)) for i in idx]
+            for _ in range(3):           # plain, captured, replayed
+                for i, r in zip(idx, gpu.answer_batch(qs)):
+                    assert np.array_equal(cl.decode(r), recs[i])
+
+
 def test_serving_threads_match_alone(world):
     gpu, _, reqs, alone = world
     out = [None] * len(reqs)
