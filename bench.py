@@ -110,13 +110,16 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
-def measured_peaks():
+def measured_peaks(key: str = "hbm_gbs"):
+    """Measured peak (HBM GB/s, or bf16 TFLOP/s burst) from MEASURED_PEAKS.json,
+    else the fallback figures (6.8 TB/s, 1.9 PFLOP/s)."""
     path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(path):
         with open(path) as f:
             d = json.load(f)
-        return float(d["hbm_gbs"]), "measured"
-    return 6800.0, "fallback"
+        if key in d:
+            return float(d[key]), "measured"
+    return (6800.0 if key == "hbm_gbs" else 1900.0), "fallback"
 
 
 def ncu_traffic():
@@ -282,22 +285,38 @@ def run_gpu(args, rank, world, local):
     # batched answering (B queries per pipeline run), same database
     batched = None
     if args.batched > 1:
-        gpu2 = SpiralGPU(p, max_batch=args.batched)
+        sizes = [args.batched, 2 * args.batched]
+        gpu2 = SpiralGPU(p, max_batch=max(sizes))
         gpu2.set_client_keys(1, keys)
         gpu2.load_db(1, recs, sh.nu1, sh.nu2)
-        for s in range(args.batched):
-            gpu2.stage_query(s, 1, 1, queries[s % len(queries)])
-        gpu2.time_staged(args.batched, 1)
-        bms = gpu2.time_staged(args.batched, max(2, args.steps // 4))
-        gpu2.stats_reset()
-        gpu2.run_staged(args.batched)
-        bsplit = gpu2.stats()
-        rb = gpu2.fetch_response(3 % args.batched)
-        assert np.array_equal(cl.decode(rb), recs[idx[3 % args.batched % len(idx)]])
-        batched = {"B": args.batched, "queries_per_s": args.batched / (bms / 1e3),
-                   "ms_per_batch": bms, "speedup_vs_single": (args.batched / bms) / (batch / ms),
-                   "stages_ms": {k[3:]: bsplit[k] for k in
-                                 ("ms_expand", "ms_convert", "ms_db_mul", "ms_fold", "ms_pack", "ms_total")}}
+        batched = []
+        for B in sizes:
+            for s in range(B):
+                gpu2.stage_query(s, 1, 1, queries[s % len(queries)])
+            gpu2.time_staged(B, 2)
+            bms = gpu2.time_staged(B, max(2, args.steps // 4))
+            gpu2.stats_reset()
+            gpu2.run_staged(B)
+            bsplit = gpu2.stats()
+            rb = gpu2.fetch_response(3 % B)
+            assert np.array_equal(cl.decode(rb), recs[idx[3 % B % len(idx)]])
+            entry = {"B": B, "queries_per_s": B / (bms / 1e3), "ms_per_batch": bms,
+                     "speedup_vs_single": (B / bms) / (batch / ms),
+                     "db_mul_variant": 1 + int(np.argmax(bsplit["db_mul_by_variant"])),
+                     "stages_ms": {k[3:]: bsplit[k] for k in
+                                   ("ms_expand", "ms_convert", "ms_db_mul", "ms_fold", "ms_pack", "ms_total")}}
+            # tensor-core multiply alone: exact fp16 digit products, 16 per
+            # residue product (4 x 4 digits), 2 ciphertext rows, B queries
+            gpu2.set_db_mul_variant(3)
+            tc_ms = gpu2.time_db_mul(1, B, 3)
+            gpu2.set_db_mul_variant(0)
+            flops = 2.0 * 16 * 2 * B * (sh.num_records * p.T * 2048 * 2)
+            tpeak, tkind = measured_peaks("bf16_tflops")
+            entry["roofline_tc"] = {"bound": "tensor", "kernel": "k_db_mul_tc (+ digit split, transpose)",
+                                    "achieved": flops / (tc_ms / 1e3) / 1e12, "peak": tpeak, "unit": "TFLOP/s",
+                                    "frac": flops / (tc_ms / 1e3) / 1e12 / tpeak, "peak_source": tkind,
+                                    "flops_per_launch": flops, "launch_ms": tc_ms}
+            batched.append(entry)
         gpu2.close()
 
     value = batch * 1e3 / ms * world

@@ -803,6 +803,124 @@ int sp_db_load_ntt(sp_ctx *c, int32_t db_id, const uint32_t *planes, int32_t nu1
     return SP_OK;
 }
 
+// ------------------------------------------------------------ checkpoints
+namespace {
+
+struct ImageHeader {
+    char magic[8];          // "SPIRDB1"
+    uint32_t version;       // 1
+    uint32_t layout;        // 1: u32 residues [prime][z][combo block][row][combo]
+    int32_t n, pt_bits, nu1, nu2;
+    uint32_t d, q1, q2;
+    uint32_t reserved;
+    uint64_t image_bytes;
+    uint64_t fnv;           // FNV-1a 64 over the image's 64-bit words
+};
+static_assert(sizeof(ImageHeader) == 64, "image header is 64 bytes");
+
+constexpr char IMAGE_MAGIC[8] = {'S', 'P', 'I', 'R', 'D', 'B', '1', 0};
+constexpr uint64_t FNV_OFFSET = 1469598103934665603ull, FNV_PRIME = 1099511628211ull;
+
+// FNV-1a over little-endian 64-bit words (n is a multiple of 8).
+uint64_t fnv1a(uint64_t h, const uint8_t *p, uint64_t n) {
+    for (uint64_t i = 0; i + 8 <= n; i += 8) {
+        uint64_t w;
+        memcpy(&w, p + i, 8);
+        h = (h ^ w) * FNV_PRIME;
+    }
+    return h;
+}
+
+struct File {
+    FILE *f = nullptr;
+    ~File() {
+        if (f) fclose(f);
+    }
+};
+
+constexpr uint64_t CKPT_CHUNK = 64ull << 20;
+
+}  // namespace
+
+int sp_db_save(sp_ctx *c, int32_t db_id, const char *path) {
+    if (!c || !path) return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    auto it = c->dbs.find(db_id);
+    if (it == c->dbs.end()) return fail(SP_ERR_NOT_FOUND, "unknown database id");
+    const Db &db = it->second;
+    TRY(sync_all(c));
+    TRY(ensure_staging(c, CKPT_CHUNK));
+    File out;
+    out.f = fopen(path, "wb");
+    if (!out.f) return fail(SP_ERR_IO, std::string("cannot open ") + path + " for writing");
+    ImageHeader h{};
+    memcpy(h.magic, IMAGE_MAGIC, 8);
+    h.version = 1;
+    h.layout = 1;
+    h.n = c->sp.n;
+    h.pt_bits = c->sp.pt_bits;
+    h.nu1 = db.L.nu1;
+    h.nu2 = db.L.nu2;
+    h.d = D;
+    h.q1 = QP0;
+    h.q2 = QP1;
+    h.image_bytes = db.bytes;
+    h.fnv = FNV_OFFSET;
+    // header first (checksum patched in at the end)
+    if (fwrite(&h, sizeof h, 1, out.f) != 1) return fail(SP_ERR_IO, std::string("cannot write ") + path);
+    const uint8_t *src = reinterpret_cast<const uint8_t *>(db.d);
+    for (uint64_t off = 0; off < db.bytes; off += CKPT_CHUNK) {
+        const uint64_t n = std::min(CKPT_CHUNK, db.bytes - off);
+        CU(cudaMemcpyAsync(c->h_stage, src + off, n, cudaMemcpyDeviceToHost, c->st));
+        CU(cudaStreamSynchronize(c->st));
+        h.fnv = fnv1a(h.fnv, c->h_stage, n);
+        if (fwrite(c->h_stage, 1, n, out.f) != n) return fail(SP_ERR_IO, std::string("cannot write ") + path);
+    }
+    if (fseek(out.f, 0, SEEK_SET) != 0 || fwrite(&h, sizeof h, 1, out.f) != 1 || fflush(out.f) != 0)
+        return fail(SP_ERR_IO, std::string("cannot write ") + path);
+    return SP_OK;
+}
+
+int sp_db_restore(sp_ctx *c, int32_t db_id, const char *path) {
+    if (!c || !path) return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    File in;
+    in.f = fopen(path, "rb");
+    if (!in.f) return fail(SP_ERR_IO, std::string("cannot open ") + path);
+    ImageHeader h{};
+    if (fread(&h, sizeof h, 1, in.f) != 1 || memcmp(h.magic, IMAGE_MAGIC, 8) != 0 || h.version != 1 ||
+        h.layout != 1)
+        return fail(SP_ERR_INVALID, std::string(path) + " is not a database image of this library");
+    if (h.d != (uint32_t)D || h.q1 != QP0 || h.q2 != QP1 || h.n != c->sp.n || h.pt_bits != c->sp.pt_bits)
+        return fail(SP_ERR_INVALID, "database image was written for other ring or plaintext parameters");
+    const DbLayout L = make_db_layout(c->sp.T, h.nu1, h.nu2);
+    if (h.nu1 < 1 || h.nu2 < 1 || h.nu1 > 14 || h.nu2 > 14 || h.image_bytes != L.words * 8)
+        return fail(SP_ERR_INVALID, "database image header does not describe a valid shape");
+    Db db;
+    TRY(db_alloc(c, db_id, h.nu1, h.nu2, db));
+    int rc = ensure_staging(c, CKPT_CHUNK);
+    uint64_t fnv = FNV_OFFSET;
+    uint8_t *dst = reinterpret_cast<uint8_t *>(db.d);
+    for (uint64_t off = 0; off < db.bytes && !rc; off += CKPT_CHUNK) {
+        const uint64_t n = std::min(CKPT_CHUNK, db.bytes - off);
+        if (fread(c->h_stage, 1, n, in.f) != n) {
+            rc = fail(SP_ERR_INVALID, std::string(path) + " is shorter than its header says");
+            break;
+        }
+        fnv = fnv1a(fnv, c->h_stage, n);
+        cudaError_t e = cudaMemcpyAsync(dst + off, c->h_stage, n, cudaMemcpyHostToDevice, c->st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+        if (e != cudaSuccess) rc = fail(SP_ERR_CUDA, std::string("database restore: ") + cudaGetErrorString(e));
+    }
+    if (!rc && fnv != h.fnv) rc = fail(SP_ERR_INVALID, std::string(path) + ": image checksum mismatch");
+    if (rc) {
+        release(c, db.d, db.bytes);
+        return rc;
+    }
+    c->dbs[db_id] = db;
+    return SP_OK;
+}
+
 int sp_db_unload(sp_ctx *c, int32_t db_id) {
     if (!c) return fail(SP_ERR_INVALID, "NULL context");
     std::lock_guard<std::mutex> lk(c->mu);

@@ -95,6 +95,8 @@ _SIGS = {
     "sp_db_mul": [_P, _I, _P, _P],
     "sp_db_mul_batch": [_P, _I, _I, _P, _P],
     "sp_set_graphs": [_P, _I],
+    "sp_db_save": [_P, _I, ctypes.c_char_p],
+    "sp_db_restore": [_P, _I, ctypes.c_char_p],
     "sp_fold": [_P, _P, _P, _I, _I, _P],
     "sp_fold_noalloc": [_P, _P, _P, _I, _I, _P],
     "sp_pack": [_P, _I, _P, _P, _U64],
@@ -183,6 +185,14 @@ class SpiralGPU:
     def load_db_ntt(self, db_id: int, planes: np.ndarray, nu1: int, nu2: int) -> None:
         pl = np.ascontiguousarray(planes, dtype=np.uint32)
         _check(self.lib.sp_db_load_ntt(self.h, db_id, _ptr(pl), nu1, nu2))
+
+    def save_db(self, db_id: int, path: str) -> None:
+        """Write database `db_id`'s encoded device image to `path`."""
+        _check(self.lib.sp_db_save(self.h, db_id, os.fsencode(path)))
+
+    def restore_db(self, db_id: int, path: str) -> None:
+        """Load an image written by save_db as database `db_id` (no encode)."""
+        _check(self.lib.sp_db_restore(self.h, db_id, os.fsencode(path)))
 
     def unload_db(self, db_id: int) -> None:
         _check(self.lib.sp_db_unload(self.h, db_id))

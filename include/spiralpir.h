@@ -38,6 +38,7 @@ extern "C" {
 #define SP_ERR_NOT_FOUND 4   /* unknown database or client id */
 #define SP_ERR_DEVICE 5      /* a device-side check failed (bounded wait ran out) */
 #define SP_ERR_UNSUPPORTED 6 /* parameter combination not implemented */
+#define SP_ERR_IO 7          /* a file could not be opened, read or written */
 
 #define SP_D 2048
 
@@ -102,6 +103,16 @@ int sp_db_load_plain(sp_ctx *ctx, int32_t db_id, const uint8_t *records, uint64_
  * gpu-pir/structures.cuh:200-210, load_db gpu-pir/db_mul_test.cu:23-34). */
 int sp_db_load_ntt(sp_ctx *ctx, int32_t db_id, const uint32_t *planes, int32_t nu1, int32_t nu2);
 int sp_db_unload(sp_ctx *ctx, int32_t db_id);
+/* Checkpoint of an encoded database image (no counterpart in the reference,
+ * which has no encoder).  sp_db_save writes a 64-byte header (magic
+ * "SPIRDB1", version, layout, n, pt_bits, nu1, nu2, d, q1, q2, image bytes,
+ * FNV-1a-64 over the image's 64-bit words) followed by the device image;
+ * sp_db_restore loads
+ * such a file as database `db_id`, skipping the encode.  The file must match
+ * the context's n and pt_bits; a short file or a checksum mismatch gives
+ * SP_ERR_INVALID and loads nothing, file errors SP_ERR_IO. */
+int sp_db_save(sp_ctx *ctx, int32_t db_id, const char *path);
+int sp_db_restore(sp_ctx *ctx, int32_t db_id, const char *path);
 
 /* ------------------------------------------------------------------ */
 /* Client public parameters, uint64 CRT form (load_polys(.., crt_form, montgomery)
