@@ -121,6 +121,7 @@ struct TicketState {
     int done = 0;
     int status = 0;
     uint8_t *response = nullptr;
+    std::chrono::steady_clock::time_point submitted, completed;
 };
 
 }  // namespace
@@ -142,10 +143,11 @@ struct sp_ctx {
     uint64_t clock = 0;
     std::mutex mu;
     sp_stats_out stats{};
-    // multiply variant chosen per (database id, queries in the launch):
+    // multiply variant chosen per (database id, size class ceil(log2 nq)):
     // 1 = per-query streaming kernel, 2 = batched integer kernel,
-    // 3 = tensor-core kernel
+    // 3 = tensor-core kernel; and the per-query kernel's one-query time
     std::map<std::pair<int, int>, int> mul_choice;
+    std::map<int, float> mul_single_ms;
     int mul_force = 0;          // 0 = autotune, 1..3 = force a variant
     bool use_graphs = true;     // replay the answer pipeline as CUDA graphs
     // serving (continuous batching)
@@ -334,6 +336,14 @@ void clear_all_graphs(sp_ctx *c) {
     for (Lane *l : c->lanes) clear_graphs(*l);
 }
 
+// A database id that is reloaded may change shape: forget its tuning.
+void forget_db(sp_ctx *c, int db_id) {
+    clear_all_graphs(c);
+    for (auto it = c->mul_choice.begin(); it != c->mul_choice.end();)
+        it = it->first.first == db_id ? c->mul_choice.erase(it) : std::next(it);
+    c->mul_single_ms.erase(db_id);
+}
+
 // Wait for the GPU work of every lane (before freeing keys or databases).
 int sync_all(sp_ctx *c) {
     if (c->main.st) CU(cudaStreamSynchronize(c->main.st));
@@ -425,11 +435,26 @@ cudaError_t launch_mul_variant(Lane &L, const Db &db, const QDesc *qd, int nq, i
     }
 }
 
-// Autotuner of the first-dimension multiply: the first time a database is
-// multiplied for `nq` queries in one launch, every available variant runs
-// once on the (already staged) selectors and the fastest, by CUDA events, is
-// kept.  Their outputs are identical; the timed runs are overwritten by the
-// real one.
+// Autotuner of the first-dimension multiply.  The choice is kept per
+// database and size class of the launch (ceil(log2 nq)).  The per-query
+// streaming variant costs nq image passes, so it is estimated as nq times its
+// one-query time, measured once per database; the best batched candidate
+// (the tensor-core kernel where the shape allows it, else the integer batch
+// kernel) runs once on the staged selectors and is timed with CUDA events.
+// Outputs are identical; the timed runs are overwritten by the real one.
+int time_variant(sp_ctx *c, Lane &L, const Db &db, const QDesc *qd, int nq, int variant, float *ms) {
+    cudaEvent_t e[2];
+    for (auto &x : e) CU(cudaEventCreate(&x));
+    cudaError_t err = cudaEventRecord(e[0], L.st);
+    if (!err) err = launch_mul_variant(L, db, qd, nq, variant);
+    if (!err) err = cudaEventRecord(e[1], L.st);
+    if (!err) err = cudaEventSynchronize(e[1]);
+    if (!err) err = cudaEventElapsedTime(ms, e[0], e[1]);
+    for (auto &x : e) cudaEventDestroy(x);
+    if (err) return fail(SP_ERR_CUDA, std::string("multiply autotune: ") + cudaGetErrorString(err));
+    return SP_OK;
+}
+
 int choose_mul_variant(sp_ctx *c, Lane &L, int db_id, const Db &db, const QDesc *qd, int nq, int *variant) {
     if (c->mul_force && variant_available(c, L, db, nq, c->mul_force)) {
         *variant = c->mul_force;
@@ -439,30 +464,25 @@ int choose_mul_variant(sp_ctx *c, Lane &L, int db_id, const Db &db, const QDesc 
         *variant = 1;
         return SP_OK;
     }
-    auto key = std::make_pair(db_id, nq);
+    const int cls = ceil_log2((uint64_t)nq);
+    auto key = std::make_pair(db_id, cls);
     auto it = c->mul_choice.find(key);
     if (it != c->mul_choice.end() && variant_available(c, L, db, nq, it->second)) {
         *variant = it->second;
         return SP_OK;
     }
+    const int cand = variant_available(c, L, db, nq, 3) ? 3 : (variant_available(c, L, db, nq, 2) ? 2 : 0);
     int best = 1;
-    float best_ms = 0;
-    for (int v = 1; v <= 3; v++) {
-        if (!variant_available(c, L, db, nq, v)) continue;
-        cudaEvent_t e[2];
-        for (auto &x : e) CU(cudaEventCreate(&x));
-        cudaError_t err = cudaEventRecord(e[0], L.st);
-        if (!err) err = launch_mul_variant(L, db, qd, nq, v);
-        if (!err) err = cudaEventRecord(e[1], L.st);
-        if (!err) err = cudaEventSynchronize(e[1]);
-        float ms = 0;
-        if (!err) err = cudaEventElapsedTime(&ms, e[0], e[1]);
-        for (auto &x : e) cudaEventDestroy(x);
-        if (err) return fail(SP_ERR_CUDA, std::string("multiply autotune: ") + cudaGetErrorString(err));
-        if (v == 1 || ms < best_ms) {
-            best = v;
-            best_ms = ms;
+    if (cand) {
+        auto one = c->mul_single_ms.find(db_id);
+        if (one == c->mul_single_ms.end()) {
+            float ms1 = 0;
+            TRY(time_variant(c, L, db, qd, 1, 1, &ms1));
+            one = c->mul_single_ms.emplace(db_id, ms1).first;
         }
+        float msb = 0;
+        TRY(time_variant(c, L, db, qd, nq, cand, &msb));
+        if (msb < one->second * nq) best = cand;
     }
     *variant = best;
     c->mul_choice[key] = best;
@@ -727,7 +747,7 @@ static int db_alloc(sp_ctx *c, int db_id, int nu1, int nu2, Db &db) {
     TRY(db_check_shape(c, nu1, nu2));
     if (c->dbs.count(db_id)) {
         TRY(sync_all(c));
-        clear_all_graphs(c);
+        forget_db(c, db_id);
         release(c, c->dbs[db_id].d, c->dbs[db_id].bytes);
         c->dbs.erase(db_id);
     }
@@ -927,7 +947,7 @@ int sp_db_unload(sp_ctx *c, int32_t db_id) {
     auto it = c->dbs.find(db_id);
     if (it == c->dbs.end()) return fail(SP_ERR_NOT_FOUND, "unknown database id");
     TRY(sync_all(c));
-    clear_all_graphs(c);
+    forget_db(c, db_id);
     release(c, it->second.d, it->second.bytes);
     c->dbs.erase(it);
     return SP_OK;
@@ -1533,6 +1553,7 @@ void complete(sp_ctx *c, uint64_t ticket, int status) {
     if (it != c->tickets.end()) {
         it->second.done = 1;
         it->second.status = status;
+        it->second.completed = std::chrono::steady_clock::now();
     }
 }
 
@@ -1650,6 +1671,12 @@ int sp_serve_start(sp_ctx *c, int32_t lanes) {
         Lane *L = new Lane();
         int rc = lane_init(c, *L, c->p.max_batch);
         if (!rc && need.g) rc = ensure_slots(c, *L, need, c->p.max_batch);
+        // then, where the budget allows, the tensor-core multiply workspace
+        // for every database that can use it (best effort: without it the
+        // lane uses the integer multiplies)
+        if (!rc && c->p.max_batch >= 2)
+            for (auto &kv : c->dbs)
+                if (db_mul_tc_supported(kv.second.L)) ensure_limbs(c, *L, kv.second.L);
         c->lanes.push_back(L);
         if (rc) {
             for (Lane *x : c->lanes) {
@@ -1700,6 +1727,7 @@ int sp_submit(sp_ctx *c, const sp_request *req, uint64_t *ticket) {
     p.response_len = req->response_len;
     TicketState ts;
     ts.response = req->response;
+    ts.submitted = std::chrono::steady_clock::now();
     c->tickets[p.ticket] = ts;
     *ticket = p.ticket;
     c->queue.push_back(std::move(p));
@@ -1719,12 +1747,19 @@ int sp_poll(sp_ctx *c, uint64_t ticket, int32_t *done, int32_t *status) {
 }
 
 int sp_wait(sp_ctx *c, uint64_t ticket, int32_t *status) {
-    if (!c || !status) return fail(SP_ERR_INVALID, "NULL argument");
+    double ms = 0;
+    return sp_wait_timed(c, ticket, status, &ms);
+}
+
+int sp_wait_timed(sp_ctx *c, uint64_t ticket, int32_t *status, double *server_ms) {
+    if (!c || !status || !server_ms) return fail(SP_ERR_INVALID, "NULL argument");
     std::unique_lock<std::mutex> lk(c->mu);
     auto it = c->tickets.find(ticket);
     if (it == c->tickets.end()) return fail(SP_ERR_NOT_FOUND, "unknown ticket");
     c->cv.wait(lk, [&] { return c->tickets[ticket].done != 0; });
-    *status = c->tickets[ticket].status;
+    const TicketState &ts = c->tickets[ticket];
+    *status = ts.status;
+    *server_ms = std::chrono::duration<double, std::milli>(ts.completed - ts.submitted).count();
     c->tickets.erase(ticket);
     return SP_OK;
 }

@@ -82,6 +82,7 @@ _SIGS = {
     "sp_submit": [_P, ctypes.POINTER(SpRequest), ctypes.POINTER(_U64)],
     "sp_poll": [_P, _U64, ctypes.POINTER(_I), ctypes.POINTER(_I)],
     "sp_wait": [_P, _U64, ctypes.POINTER(_I)],
+    "sp_wait_timed": [_P, _U64, ctypes.POINTER(_I), ctypes.POINTER(ctypes.c_double)],
     "sp_serve_stats": [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64), ctypes.POINTER(_U64)],
     "sp_stats": [_P, ctypes.POINTER(SpStats)],
     "sp_stats_reset": [_P],

@@ -146,15 +146,16 @@ int sp_fetch_response(sp_ctx *ctx, int32_t slot, uint8_t *response, uint64_t res
 int sp_time_staged(sp_ctx *ctx, int32_t count, int32_t iters, double *ms_per_run);
 
 /* First-dimension multiply variant for launches with several queries on one
- * database: 0 = autotune (default: time every available variant once per
- * database and batch size, keep the fastest), 1 = per-query streaming kernel
- * (TMA-fed, HBM-bound), 2 = batched integer kernel (each residue read once per
- * 8 queries), 3 = tensor-core kernel (exact fp16 digit products, up to 32
- * queries per pass over the image; needs 128 combos per block and at most
- * 512 rows, and a workspace of rows * 2 MiB + up to 512 MiB per pipeline
- * lane).  A forced variant that does
- * not apply falls back to the autotuner.  sp_time_db_mul times the forced
- * variant (1 when none is forced).  The result is identical. */
+ * database: 0 = autotune (default: per database and size class ceil(log2 nq),
+ * the best batched candidate is timed once against nq times the per-query
+ * kernel's one-query time, and the faster is kept), 1 = per-query streaming
+ * kernel (TMA-fed, HBM-bound), 2 = batched integer kernel (each residue read
+ * once per 8 queries), 3 = tensor-core kernel (exact fp16 digit products, up
+ * to 32 queries per pass over the image; needs 128 combos per block and at
+ * most 512 rows, and a workspace of rows * 2 MiB + up to 512 MiB per pipeline
+ * lane).  A forced variant that does not apply falls back to the autotuner.
+ * sp_time_db_mul times the forced variant (1 when none is forced).  The
+ * result is identical. */
 int sp_set_db_mul_variant(sp_ctx *ctx, int32_t variant);
 /* Answer pipelines run as CUDA graphs (default on): the launches of a batch
  * plan (query count, expansion and fold depths, and the database, length and
@@ -178,6 +179,9 @@ int sp_serve_stop(sp_ctx *ctx);
 int sp_submit(sp_ctx *ctx, const sp_request *req, uint64_t *ticket);
 int sp_poll(sp_ctx *ctx, uint64_t ticket, int32_t *done, int32_t *status);
 int sp_wait(sp_ctx *ctx, uint64_t ticket, int32_t *status);
+/* sp_wait that also returns the request's server-side latency: milliseconds
+ * from sp_submit to the response bytes being written (steady clock). */
+int sp_wait_timed(sp_ctx *ctx, uint64_t ticket, int32_t *status, double *server_ms);
 int sp_serve_stats(sp_ctx *ctx, uint64_t *served, uint64_t *batches, uint64_t *queued);
 
 int sp_stats(sp_ctx *ctx, sp_stats_out *out);

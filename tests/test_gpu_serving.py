@@ -182,3 +182,24 @@ def test_invalid_shape_rejected():
         with pytest.raises(SpiralError) as e:
             gpu.load_db(1, np.zeros((1 << 14, 4, 2048), np.uint8), 3, 11)
         assert e.value.code == 6
+
+
+def test_production_parameter_set():
+    """The larger parameter set of gpu-pir/params.cuh:57-62 (t_exp_left = 16,
+    t_exp_right = 56, t_gsw = 7, t_conv = 4, nu1 = 10, nu2 = 4: 1024 rows,
+    11 expansion rounds, 1-bit right-branch digits): answers alone and in a
+    batch are identical and decode to the records."""
+    p = P.SpiralParams(n=2, pt_bits=8, t_exp_left=16, t_exp_right=56, t_gsw=7, t_conv=4, q2_bits=22)
+    sh = P.DbShape(10, 4)
+    recs = C.random_records(sh, p, seed=111)
+    cl = C.Client(p, seed=112)
+    with SpiralGPU(p, max_batch=4) as gpu:
+        gpu.set_client_keys(1, cl.public_keys(sh.nu1, sh.nu2))
+        gpu.load_db(1, recs, sh.nu1, sh.nu2)
+        idx = [0, 12345, sh.num_records - 1, 777]
+        qs = [cl.query(sh, i) for i in idx]
+        alone = [gpu.answer(1, 1, q) for q in qs]
+        for i, r in zip(idx, alone):
+            assert np.array_equal(cl.decode(r), recs[i])
+        for x, y in zip(gpu.answer_batch([(1, 1, q) for q in qs]), alone):
+            assert np.array_equal(x, y)
