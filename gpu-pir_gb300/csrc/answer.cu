@@ -4,6 +4,8 @@
 // CTA shape everywhere: 256 threads = two NTT groups of 128; group g works
 // modulo prime g.  Raw (56-bit) values are rebuilt by an inverse CRT of both
 // groups' INTT outputs exchanged through shared memory.
+#include <algorithm>
+
 #include "answer.cuh"
 
 namespace sp {
@@ -144,9 +146,13 @@ cudaError_t launch_widen(const uint32_t *in, uint64_t *out, uint64_t planes, boo
 template <int GP>
 __global__ void __launch_bounds__(256 * GP, 3 - GP) k_expand_round(const QDesc *__restrict__ qd, int r, StageParams sp,
                                                           const TwiddleSet *__restrict__ tws,
-                                                          const uint32_t *__restrict__ neg1) {
+                                                          const uint32_t *__restrict__ neg1, int split,
+                                                          uint32_t *__restrict__ part,
+                                                          unsigned int *__restrict__ counters) {
     const QDesc &Q = qd[blockIdx.y];
-    const int i = blockIdx.x;
+    const int items = gridDim.x / split;
+    const int i = blockIdx.x / split, s = blockIdx.x % split;
+    __shared__ int s_last;
     if (!Q.active || r >= Q.g || i >= (2 << r)) return;
     const int max_bits = sp.t_gsw * Q.nu2;
     if (Q.stop > 0 && r > Q.stop && (i & 1)) return;
@@ -199,7 +205,7 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_expand_round(const QDesc *
 #pragma unroll
     for (int j = 0; j < VPT; j++) acc0[j] = acc1[j] = 0;
 #pragma unroll 1
-    for (int k = sub; k < tk; k += GP) {
+    for (int k = s * GP + sub; k < tk; k += GP * split) {
         uint32_t d[VPT];
 #pragma unroll
         for (int j = 0; j < VPT; j++) d[j] = (uint32_t)((raws[t + GROUP * j] >> (bits * k)) & mask);
@@ -217,6 +223,27 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_expand_round(const QDesc *
         for (int j = 0; j < VPT; j++) {
             if (sub == 0) acc0[j] = reduce2(acc0[j] + w[j], 2 * c.p);
             else acc1[j] = reduce2(acc1[j] + w[j], 2 * c.p);
+        }
+        if (split > 1) {
+            // publish this CTA's partial of row `sub`; the last CTA of the
+            // output sums the others' and writes the output
+            uint32_t(&a)[VPT] = sub == 0 ? acc0 : acc1;
+            const size_t slot0 = ((size_t)blockIdx.y * items + i) * split;
+            st16(part + ((slot0 + s) * 4 + g * 2 + sub) * D + VPT * t, a);
+            __threadfence();
+            __syncthreads();
+            if (threadIdx.x == 0)
+                s_last = atomicAdd(&counters[(size_t)blockIdx.y * items + i], 1u) == (unsigned)(split - 1);
+            __syncthreads();
+            if (!s_last) return;
+            __threadfence();
+            for (int s2 = 0; s2 < split; s2++) {
+                if (s2 == s) continue;
+                ld16_l2(w, part + ((slot0 + s2) * 4 + g * 2 + sub) * D + VPT * t);
+#pragma unroll
+                for (int j = 0; j < VPT; j++) a[j] = reduce2(a[j] + w[j], 2 * c.p);
+            }
+            if (threadIdx.x == 0) counters[(size_t)blockIdx.y * items + i] = 0;   // ready for the next launch
         }
     }
     // output rows: row 0 = v.row0 + acc0, row 1 = v.row1 + acc1 + tau(v.row1)
@@ -255,18 +282,31 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_expand_round(const QDesc *
 }
 
 cudaError_t launch_expand_round(const QDesc *qd, int nq, int r, int max_out, const StageParams &sp,
-                                const TwiddleSet *tw, const uint32_t *neg1, cudaStream_t st) {
-    const bool wide = (uint64_t)max_out * nq < 2ull * sm_count();
-    if (wide) {
+                                const TwiddleSet *tw, const uint32_t *neg1, const SplitScratch *scr,
+                                cudaStream_t st) {
+    const uint64_t total = (uint64_t)max_out * nq;
+    const int sms = sm_count();
+    if (total < 2ull * sms) {
+        // few outputs: 2 groups per prime split the digits; with scratch,
+        // each output also spreads over `split` CTAs while that stays within
+        // one CTA per SM, at least one digit transform per group
+        int split = 1;
+        if (scr && scr->part) {
+            const int digits = std::max(sp.t_left, sp.t_right);
+            split = (int)std::min<uint64_t>(std::max<uint64_t>(1, sms / total), (uint64_t)(digits + 1) / 2);
+            while (split > 1 && (total * split > (uint64_t)scr->slots || total > (uint64_t)scr->counter_slots)) split--;
+        }
         const int smem = (TW_WORDS + 4 * 2 * D) * 4 + D * 8;
         cudaError_t e = cudaFuncSetAttribute(k_expand_round<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
-        k_expand_round<2><<<dim3(max_out, nq), 512, smem, st>>>(qd, r, sp, tw, neg1);
+        k_expand_round<2><<<dim3(max_out * split, nq), 512, smem, st>>>(qd, r, sp, tw, neg1, split,
+                                                                        scr ? scr->part : nullptr,
+                                                                        scr ? scr->counters : nullptr);
     } else {
         const int smem = SMEM_BYTES + D * 8;
         cudaError_t e = cudaFuncSetAttribute(k_expand_round<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
-        k_expand_round<1><<<dim3(max_out, nq), THREADS, smem, st>>>(qd, r, sp, tw, neg1);
+        k_expand_round<1><<<dim3(max_out, nq), THREADS, smem, st>>>(qd, r, sp, tw, neg1, 1, nullptr, nullptr);
     }
     return cudaGetLastError();
 }
@@ -420,12 +460,17 @@ cudaError_t launch_gsw_neg(const uint32_t *gsw, uint32_t *neg, int count, int t,
 // GP = 2 halves the latency of a fold and is used when a level has few folds.
 template <int GP>
 __global__ void __launch_bounds__(256 * GP, 3 - GP) k_fold_level(const QDesc *__restrict__ qd, int level, StageParams sp,
-                                                        const TwiddleSet *__restrict__ tws) {
+                                                        const TwiddleSet *__restrict__ tws, int split,
+                                                        uint32_t *__restrict__ part,
+                                                        unsigned int *__restrict__ counters) {
     const QDesc &Q = qd[blockIdx.y];
     if (!Q.active || level >= Q.nu2) return;
+    const int items = gridDim.x / split;
+    const int item = blockIdx.x / split, s = blockIdx.x % split;
     const int num_per = 1 << (Q.nu2 - 1 - level);
-    const int inst = blockIdx.x / num_per, i = blockIdx.x % num_per;
+    const int inst = item / num_per, i = item % num_per;
     if (inst >= sp.T) return;
+    __shared__ int s_last;
     extern __shared__ __align__(16) uint32_t smem[];
     load_twiddles(smem, tws);
     const int gi = threadIdx.x >> 7, g = gi & 1, sub = gi >> 1, t = threadIdx.x & (GROUP - 1), bar = 1 + gi;
@@ -446,7 +491,7 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_fold_level(const QDesc *__
 #pragma unroll
     for (int j = 0; j < VPT; j++) acc0[j] = acc1[j] = 0;
 #pragma unroll 1
-    for (int pr = sub; pr < 2 * tg; pr += GP) {
+    for (int pr = s * GP + sub; pr < 2 * tg; pr += GP * split) {
         const int row = pr / tg, k = pr % tg;
         const int sh = bits * k;
         uint32_t d[VPT];
@@ -492,6 +537,25 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_fold_level(const QDesc *__
 #pragma unroll
         for (int j = 0; j < VPT; j++) a[j] = reduce2((sub == 0 ? acc0[j] : acc1[j]) + w[j], 2 * c.p);
         __syncthreads();   // partner has read this group's buffer
+        if (split > 1) {
+            // publish this CTA's partial; the last CTA of the item finishes it
+            const size_t slot0 = ((size_t)blockIdx.y * items + item) * split;
+            st16(part + ((slot0 + s) * 4 + g * 2 + sub) * D + VPT * t, a);
+            __threadfence();
+            __syncthreads();
+            if (threadIdx.x == 0)
+                s_last = atomicAdd(&counters[(size_t)blockIdx.y * items + item], 1u) == (unsigned)(split - 1);
+            __syncthreads();
+            if (!s_last) return;
+            __threadfence();
+            for (int s2 = 0; s2 < split; s2++) {
+                if (s2 == s) continue;
+                ld16_l2(w, part + ((slot0 + s2) * 4 + g * 2 + sub) * D + VPT * t);
+#pragma unroll
+                for (int j = 0; j < VPT; j++) a[j] = reduce2(a[j] + w[j], 2 * c.p);
+            }
+            if (threadIdx.x == 0) counters[(size_t)blockIdx.y * items + item] = 0;   // ready for the next launch
+        }
         ntt_inv(a, twi, buf, c, t, bar);
         group_sync(bar);
 #pragma unroll
@@ -510,17 +574,29 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_fold_level(const QDesc *__
 }
 
 cudaError_t launch_fold_level(const QDesc *qd, int nq, int level, int max_items, const StageParams &sp,
-                              const TwiddleSet *tw, cudaStream_t st) {
-    const bool wide = (uint64_t)max_items * nq < 2ull * sm_count();
-    if (wide) {
+                              const TwiddleSet *tw, const SplitScratch *scr, cudaStream_t st) {
+    const uint64_t total = (uint64_t)max_items * nq;
+    const int sms = sm_count();
+    if (total < 2ull * sms) {
+        // few folds: 2 groups per prime split the digits; with scratch, each
+        // fold also spreads over `split` CTAs while that stays within one CTA
+        // per SM (this kernel's footprint), at least one digit transform per
+        // group
+        int split = 1;
+        if (scr && scr->part) {
+            split = (int)std::min<uint64_t>(std::max<uint64_t>(1, sms / total), (uint64_t)sp.t_gsw);
+            while (split > 1 && (total * split > (uint64_t)scr->slots || total > (uint64_t)scr->counter_slots)) split--;
+        }
         const int smem = (TW_WORDS + 4 * 2 * D) * 4;
         cudaError_t e = cudaFuncSetAttribute(k_fold_level<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
-        k_fold_level<2><<<dim3(max_items, nq), 512, smem, st>>>(qd, level, sp, tw);
+        k_fold_level<2><<<dim3(max_items * split, nq), 512, smem, st>>>(qd, level, sp, tw, split,
+                                                                         scr ? scr->part : nullptr,
+                                                                         scr ? scr->counters : nullptr);
     } else {
         cudaError_t e = cudaFuncSetAttribute(k_fold_level<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
         if (e != cudaSuccess) return e;
-        k_fold_level<1><<<dim3(max_items, nq), THREADS, SMEM_BYTES, st>>>(qd, level, sp, tw);
+        k_fold_level<1><<<dim3(max_items, nq), THREADS, SMEM_BYTES, st>>>(qd, level, sp, tw, 1, nullptr, nullptr);
     }
     return cudaGetLastError();
 }
@@ -538,15 +614,21 @@ __device__ __forceinline__ uint32_t rescale_q(uint64_t x, int bits_out) {
 
 constexpr int PACK_MAX_N = 2;
 
-// Column c = blockIdx.x of query blockIdx.y: sum over r < n of
-// W_r * NTT(G^-1(ct[r*n+c].row0)) + e_{1+r} * NTT(ct[r*n+c].row1), then raw,
-// then row 0 rescaled to 2^q2_bits and rows 1..n to 4p.
+// Column col of query blockIdx.y: sum over r < n of
+// W_r * NTT(G^-1(ct[r*n+col].row0)) + e_{1+r} * NTT(ct[r*n+col].row1), then
+// raw, then row 0 rescaled to 2^q2_bits and rows 1..n to 4p.
+// The n*(t_conv + 1) transforms of a column (digit k < t_conv of ct r's row
+// 0, or its row 1 for k = t_conv) are spread over `split` CTAs; with
+// split > 1 each CTA publishes its partial sums and the last to arrive
+// finishes the column (no CTA waits for another).
 __global__ void __launch_bounds__(THREADS, 2) k_pack(const QDesc *__restrict__ qd, StageParams sp,
-                                                 const TwiddleSet *__restrict__ tws) {
+                                                 const TwiddleSet *__restrict__ tws, int split,
+                                                 uint32_t *__restrict__ part, unsigned int *__restrict__ counters) {
     const QDesc &Q = qd[blockIdx.y];
-    const int col = blockIdx.x;
+    const int col = blockIdx.x / split, s = blockIdx.x % split;
     if (!Q.active || col >= sp.n) return;
     extern __shared__ __align__(16) uint32_t smem[];
+    __shared__ int s_last;
     const Ctx x = setup(smem, tws);
     const Prime &c = x.c;
     const int n = sp.n, tcv = sp.t_conv;
@@ -558,31 +640,58 @@ __global__ void __launch_bounds__(THREADS, 2) k_pack(const QDesc *__restrict__ q
     for (int a = 0; a <= PACK_MAX_N; a++)
 #pragma unroll
         for (int j = 0; j < VPT; j++) acc[a][j] = 0;
-    for (int r = 0; r < n; r++) {
-        const uint64_t *ct = Q.raw + (size_t)(r * n + col) * cols * 2 * D;   // folded result of instance r*n+col
-        const uint32_t *W = Q.pack + (size_t)r * (n + 1) * tcv * 2 * D;
-        uint64_t raw[VPT];
-#pragma unroll
-        for (int j = 0; j < VPT; j++) raw[j] = ct[x.t + GROUP * j];
 #pragma unroll 1
-        for (int k = 0; k < tcv; k++) {
+    for (int u = s; u < n * (tcv + 1); u += split) {
+        const int r = u / (tcv + 1), k = u % (tcv + 1);
+        const uint64_t *ct = Q.raw + (size_t)(r * n + col) * cols * 2 * D;   // folded result of instance r*n+col
+        if (k < tcv) {
+            const uint32_t *W = Q.pack + (size_t)r * (n + 1) * tcv * 2 * D;
+            uint64_t raw[VPT];
+#pragma unroll
+            for (int j = 0; j < VPT; j++) raw[j] = ct[x.t + GROUP * j];
             uint32_t d[VPT];
             digits(d, raw, bits * k, mask);
             ntt_fwd(d, tw_fwd(x), x.buf, c, x.t, x.bar);
 #pragma unroll
             for (int a = 0; a <= PACK_MAX_N; a++)
                 if (a <= n) mac16(acc[a], d, W + ((size_t)(a * tcv + k) * 2 + x.g) * D + VPT * x.t, c);
+        } else {
+            uint32_t b[VPT];
+#pragma unroll
+            for (int j = 0; j < VPT; j++) b[j] = mod_u64(ct[D + x.t + GROUP * j], c);
+            ntt_fwd(b, tw_fwd(x), x.buf, c, x.t, x.bar);
+#pragma unroll
+            for (int a = 1; a <= PACK_MAX_N; a++)
+                if (a == 1 + r) {
+#pragma unroll
+                    for (int j = 0; j < VPT; j++) acc[a][j] = reduce2(acc[a][j] + reduce2(b[j], 2 * c.p), 2 * c.p);
+                }
         }
-        uint32_t b[VPT];
+    }
+    if (split > 1) {
+        const size_t item = (size_t)blockIdx.y * n + col;
+        auto plane = [&](int s2, int a) { return part + (((item * split + s2) * (n + 1) + a) * 2 + x.g) * D + VPT * x.t; };
 #pragma unroll
-        for (int j = 0; j < VPT; j++) b[j] = mod_u64(ct[D + x.t + GROUP * j], c);
-        ntt_fwd(b, tw_fwd(x), x.buf, c, x.t, x.bar);
+        for (int a = 0; a <= PACK_MAX_N; a++)
+            if (a <= n) st16(plane(s, a), acc[a]);
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) s_last = atomicAdd(&counters[item], 1u) == (unsigned)(split - 1);
+        __syncthreads();
+        if (!s_last) return;
+        __threadfence();
+        for (int s2 = 0; s2 < split; s2++) {
+            if (s2 == s) continue;
 #pragma unroll
-        for (int a = 1; a <= PACK_MAX_N; a++)
-            if (a == 1 + r) {
+            for (int a = 0; a <= PACK_MAX_N; a++) {
+                if (a > n) break;
+                uint32_t w[VPT];
+                ld16_l2(w, plane(s2, a));
 #pragma unroll
-                for (int j = 0; j < VPT; j++) acc[a][j] = reduce2(acc[a][j] + reduce2(b[j], 2 * c.p), 2 * c.p);
+                for (int j = 0; j < VPT; j++) acc[a][j] = reduce2(acc[a][j] + w[j], 2 * c.p);
             }
+        }
+        if (threadIdx.x == 0) counters[item] = 0;   // ready for the next launch
     }
 #pragma unroll
     for (int a = 0; a <= PACK_MAX_N; a++) {
@@ -599,11 +708,22 @@ __global__ void __launch_bounds__(THREADS, 2) k_pack(const QDesc *__restrict__ q
     }
 }
 
-cudaError_t launch_pack(const QDesc *qd, int nq, const StageParams &sp, const TwiddleSet *tw, cudaStream_t st) {
-    if (sp.n > PACK_MAX_N) return cudaErrorInvalidValue;
+cudaError_t launch_pack(const QDesc *qd, int nq, const StageParams &sp, const TwiddleSet *tw,
+                        const SplitScratch *scr, cudaStream_t st) {
     cudaError_t e = cudaFuncSetAttribute(k_pack, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     if (e != cudaSuccess) return e;
-    k_pack<<<dim3(sp.n, nq), THREADS, SMEM_BYTES, st>>>(qd, sp, tw);
+    // spread each column's n*(t_conv+1) transforms over CTAs while the launch
+    // stays within the SMs and the scratch
+    const uint64_t cols = (uint64_t)sp.n * nq;
+    const int units = sp.n * (sp.t_conv + 1);
+    int split = 1;
+    if (scr && scr->part) {
+        split = (int)std::min<uint64_t>(std::max<uint64_t>(1, sm_count() / cols), (uint64_t)units);
+        while (split > 1 && (cols * split * (sp.n + 1) * 2 > (uint64_t)scr->slots * 4 || cols > (uint64_t)scr->counter_slots))
+            split--;
+    }
+    k_pack<<<dim3(sp.n * split, nq), THREADS, SMEM_BYTES, st>>>(qd, sp, tw, split, scr ? scr->part : nullptr,
+                                                               scr ? scr->counters : nullptr);
     return cudaGetLastError();
 }
 

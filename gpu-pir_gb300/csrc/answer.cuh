@@ -10,6 +10,15 @@
 
 namespace sp {
 
+// Scratch of split launches: a narrow fold level (or expansion round) may
+// run each item as `split` CTAs that transform disjoint subsets of the
+// digits; each CTA stores its partial key products and the last to arrive
+// (arrival counter per item, no waiting) sums them and finishes the item.
+struct SplitScratch {
+    uint32_t *part = nullptr;       // [slots][2 primes x 2 rows][D] partial sums
+    uint32_t *counters = nullptr;   // [counter_slots], zero between launches
+    int slots = 0, counter_slots = 0;
+};
 // u64 canonical residues [count][2][D] -> u32 (optionally Montgomery form)
 cudaError_t launch_narrow(const uint64_t *in, uint32_t *out, uint64_t planes, bool to_mont, cudaStream_t st);
 // u32 [count][2][D] (optionally from Montgomery form) -> u64 canonical
@@ -22,15 +31,17 @@ cudaError_t launch_acc_to_raw(const QDesc *qd, int nq, int max_items, const Stag
 cudaError_t launch_sel_import(const uint64_t *in, uint32_t *sel, int rows, cudaStream_t st);
 
 cudaError_t launch_expand_round(const QDesc *qd, int nq, int r, int max_out, const StageParams &sp,
-                                const TwiddleSet *tw, const uint32_t *neg1, cudaStream_t st);
+                                const TwiddleSet *tw, const uint32_t *neg1, const SplitScratch *scr,
+                                cudaStream_t st);
 cudaError_t launch_regev_to_gsw(const QDesc *qd, int nq, int max_items, const StageParams &sp,
                                 const TwiddleSet *tw, cudaStream_t st);
 // G - C for count GSW ciphertexts (canonical in and out)
 cudaError_t launch_gsw_neg(const uint32_t *gsw, uint32_t *neg, int count, int t, cudaStream_t st);
+// scr == nullptr: no split (every item in one CTA)
 cudaError_t launch_fold_level(const QDesc *qd, int nq, int level, int max_items, const StageParams &sp,
-                              const TwiddleSet *tw, cudaStream_t st);
+                              const TwiddleSet *tw, const SplitScratch *scr, cudaStream_t st);
 cudaError_t launch_pack(const QDesc *qd, int nq, const StageParams &sp, const TwiddleSet *tw,
-                        cudaStream_t st);
+                        const SplitScratch *scr, cudaStream_t st);
 cudaError_t launch_bitpack(const QDesc *qd, int nq, const StageParams &sp, uint64_t resp_bytes,
                            cudaStream_t st);
 

@@ -99,6 +99,8 @@ struct Lane {
     uint64_t limb_bytes = 0;            // tiles, then the chunk output
     uint32_t *tc_out = nullptr;
     uint64_t tc_out_bytes = 0;
+    SplitScratch split{};               // narrow fold levels split over CTAs
+    uint64_t split_bytes = 0;
     int cap = 0;
     int staged = 0;
     bool busy = false;                  // serving: a batch is in flight
@@ -294,6 +296,13 @@ int lane_init(sp_ctx *c, Lane &L, int cap) {
     memset(L.h_qd, 0, sizeof(QDesc) * cap);
     CU(cudaMallocHost(&L.h_resp, response_bytes(c->sp) * cap));
     CU(cudaMemset(L.d_err, 0, 16));
+    // split scratch: partial sums for up to 4 CTAs per SM, 4096 counters
+    L.split.slots = 4 * sm_count();
+    L.split.counter_slots = 4096;
+    L.split_bytes = (uint64_t)L.split.slots * 4 * D * 4 + (uint64_t)L.split.counter_slots * 4;
+    TRY(alloc(c, (void **)&L.split.part, L.split_bytes));
+    L.split.counters = reinterpret_cast<uint32_t *>(L.split.part + (uint64_t)L.split.slots * 4 * D);
+    CU(cudaMemset(L.split.counters, 0, (uint64_t)L.split.counter_slots * 4));
     return SP_OK;
 }
 
@@ -318,6 +327,8 @@ void lane_free(sp_ctx *c, Lane &L) {
     release(c, L.tc_out, L.tc_out_bytes);
     L.tc_out = nullptr;
     L.tc_out_bytes = 0;
+    release(c, L.split.part, L.split_bytes);
+    L.split = SplitScratch{};
     L.d_err = nullptr;
     L.d_qd = nullptr;
     if (L.h_qd) cudaFreeHost(L.h_qd);
@@ -534,7 +545,8 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot)
     auto enqueue = [&](bool capturing) -> cudaError_t {
         const unsigned ev_flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
         cudaError_t e = cudaEventRecordWithFlags(L.ev[0], st, ev_flags);
-        for (int r = 0; r < max_g && !e; r++) e = launch_expand_round(L.d_qd, nq, r, 2 << r, sp, c->d_tw, c->d_neg1, st);
+        for (int r = 0; r < max_g && !e; r++)
+            e = launch_expand_round(L.d_qd, nq, r, 2 << r, sp, c->d_tw, c->d_neg1, &L.split, st);
         if (!e) e = cudaEventRecordWithFlags(L.ev[1], st, ev_flags);
         if (!e) e = launch_regev_to_gsw(L.d_qd, nq, max_items, sp, c->d_tw, st);
         if (!e) e = cudaEventRecordWithFlags(L.ev[2], st, ev_flags);
@@ -545,9 +557,9 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot)
         if (!e) e = cudaEventRecordWithFlags(L.ev[3], st, ev_flags);
         if (!e) e = launch_acc_to_raw(L.d_qd, nq, sp.T * (2 << max_nu2), sp, c->d_tw, st);
         for (int lvl = 0; lvl < max_nu2 && !e; lvl++)
-            e = launch_fold_level(L.d_qd, nq, lvl, sp.T << (max_nu2 - 1 - lvl), sp, c->d_tw, st);
+            e = launch_fold_level(L.d_qd, nq, lvl, sp.T << (max_nu2 - 1 - lvl), sp, c->d_tw, &L.split, st);
         if (!e) e = cudaEventRecordWithFlags(L.ev[4], st, ev_flags);
-        if (!e) e = launch_pack(L.d_qd, nq, sp, c->d_tw, st);
+        if (!e) e = launch_pack(L.d_qd, nq, sp, c->d_tw, &L.split, st);
         if (!e) e = launch_bitpack(L.d_qd, nq, sp, response_bytes(sp), st);
         if (!e) e = cudaEventRecordWithFlags(L.ev[5], st, ev_flags);
         return e;
@@ -1323,7 +1335,7 @@ int sp_expand(sp_ctx *c, int32_t client_id, const uint64_t *query, int32_t nu1, 
     CU(launch_narrow(q64.as<uint64_t>(), q32.as<uint32_t>(), 4, false, c->st));
     CU(cudaMemcpyAsync(qd.p, &d, sizeof(QDesc), cudaMemcpyHostToDevice, c->st));
     for (int r = 0; r < rounds; r++)
-        CU(launch_expand_round(qd.as<QDesc>(), 1, r, 2 << r, c->sp, c->d_tw, c->d_neg1, c->st));
+        CU(launch_expand_round(qd.as<QDesc>(), 1, r, 2 << r, c->sp, c->d_tw, c->d_neg1, nullptr, c->st));
     uint32_t *fin = (rounds & 1) ? d.v[1] : d.v[0];
     // Entries pruned in the last round(s) are zero; odd entries frozen at
     // stop_round come from the capture buffer.
@@ -1483,7 +1495,7 @@ int sp_fold(sp_ctx *c, const uint64_t *cts, const uint64_t *gsw, int32_t T, int3
     CU(launch_narrow(g64.as<uint64_t>(), g.as<uint32_t>(), gwords / D, true, c->st));
     CU(cudaMemcpyAsync(qd.p, &d, sizeof(QDesc), cudaMemcpyHostToDevice, c->st));
     for (int lvl = 0; lvl < nu2; lvl++)
-        CU(launch_fold_level(qd.as<QDesc>(), 1, lvl, T << (nu2 - 1 - lvl), sp, c->d_tw, c->st));
+        CU(launch_fold_level(qd.as<QDesc>(), 1, lvl, T << (nu2 - 1 - lvl), sp, c->d_tw, nullptr, c->st));
     for (int t = 0; t < T; t++)
         CU(cudaMemcpyAsync(out + (uint64_t)t * 2 * D, r.as<uint64_t>() + ((uint64_t)t << nu2) * 2 * D, 2ull * D * 8,
                            cudaMemcpyDeviceToHost, c->st));
@@ -1513,7 +1525,7 @@ int sp_pack(sp_ctx *c, int32_t client_id, const uint64_t *cts, uint8_t *response
     d.active = 1;
     CU(cudaMemcpyAsync(r.p, cts, (uint64_t)T * 2 * D * 8, cudaMemcpyHostToDevice, c->st));
     CU(cudaMemcpyAsync(qd.p, &d, sizeof(QDesc), cudaMemcpyHostToDevice, c->st));
-    CU(launch_pack(qd.as<QDesc>(), 1, c->sp, c->d_tw, c->st));
+    CU(launch_pack(qd.as<QDesc>(), 1, c->sp, c->d_tw, nullptr, c->st));
     CU(launch_bitpack(qd.as<QDesc>(), 1, c->sp, rb, c->st));
     CU(cudaMemcpyAsync(response, resp.p, rb, cudaMemcpyDeviceToHost, c->st));
     CU(cudaStreamSynchronize(c->st));

@@ -320,6 +320,15 @@ __device__ __forceinline__ void ld16(uint32_t (&v)[VPT], const uint32_t *p) {
         v[4 * i] = x.x; v[4 * i + 1] = x.y; v[4 * i + 2] = x.z; v[4 * i + 3] = x.w;
     }
 }
+// ld16 that reads through L2 only (data another CTA wrote in this launch)
+__device__ __forceinline__ void ld16_l2(uint32_t (&v)[VPT], const uint32_t *p) {
+    const uint4 *q = reinterpret_cast<const uint4 *>(p);
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        uint4 x = __ldcg(q + i);
+        v[4 * i] = x.x; v[4 * i + 1] = x.y; v[4 * i + 2] = x.z; v[4 * i + 3] = x.w;
+    }
+}
 __device__ __forceinline__ void st16(uint32_t *p, const uint32_t (&v)[VPT]) {
     uint4 *q = reinterpret_cast<uint4 *>(p);
 #pragma unroll

@@ -92,7 +92,7 @@ extern "C" int sp_fold_noalloc(sp_ctx *ctx, const uint64_t *cts, const uint64_t 
     if (e == cudaSuccess) e = launch_narrow(d_g64, d_g32, gwords / D, true, v.st);
     if (e == cudaSuccess) e = cudaMemcpyAsync(d_qd, &d, sizeof(QDesc), cudaMemcpyHostToDevice, v.st);
     for (int lvl = 0; lvl < nu2 && e == cudaSuccess; lvl++)
-        e = launch_fold_level(d_qd, 1, lvl, T << (nu2 - 1 - lvl), sp, v.tw, v.st);
+        e = launch_fold_level(d_qd, 1, lvl, T << (nu2 - 1 - lvl), sp, v.tw, nullptr, v.st);
     for (int t = 0; t < T && e == cudaSuccess; t++)
         e = cudaMemcpyAsync(out + (uint64_t)t * 2 * D, d_raw + ((uint64_t)t << nu2) * 2 * D, 2ull * D * 8,
                             cudaMemcpyDeviceToHost, v.st);
