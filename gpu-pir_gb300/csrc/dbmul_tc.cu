@@ -84,6 +84,10 @@ struct Ctrl {
     uint64_t acc_full, acc_empty, drain;
     uint32_t tmem_base;
     int abort;
+    // drain constants per prime, computed once: weights 2^(7d) * 2^32 mod p
+    // and a multiple of p above the largest |weighted sum|
+    int32_t wts[2][7];
+    int64_t off[2];
 };
 static_assert(sizeof(Ctrl) <= 1024, "control block");
 
@@ -195,23 +199,21 @@ __device__ __forceinline__ int32_t f2i_small(uint32_t bits) {
 // class d) * 2^21, so classes 0, 1, 5, 6 (at most 2 digit pairs) convert
 // with f2i_small and classes 2, 3, 4 with cvt.
 __device__ __forceinline__ void drain_quarter(uint32_t lane_addr, int N, int c0, const DbLayout &L, int z0,
-                                              int zc, uint64_t u, int m, uint32_t *out) {
-    const int cbi = (int)(u % L.ncb);
-    const int zl = (int)((u / L.ncb) % D) - z0;
-    const int prime = (int)(u / ((uint64_t)L.ncb * D));
+                                              int zc, uint64_t u, int m, uint32_t *out, const int32_t (&wts)[2][7],
+                                              const int64_t (&offs)[2]) {
+    // unit -> (prime, slot, block) in 32-bit arithmetic (units < 2^31)
+    const uint32_t uu = (uint32_t)u, ncb = (uint32_t)L.ncb;
+    const int cbi = (int)(uu % ncb);
+    const int zl = (int)((uu / ncb) % D) - z0;
+    const int prime = (int)(uu / (ncb * D));
     const uint32_t p = prime ? QP1 : QP0;
     const uint32_t npinv = 0u - (prime ? P1_PINV : P0_PINV);
     // weights 2^(7d) * 2^32 mod p: one Montgomery reduction of the weighted
     // sum returns sum_d C_d 2^(7d) mod p
     int32_t w[7];
-    uint64_t wd = (1ull << 32) % p;
 #pragma unroll
-    for (int d = 0; d < 7; d++) {
-        w[d] = (int32_t)wd;
-        wd = (wd << 7) % p;
-    }
-    // a multiple of p above the largest |sum| (< 7 * 2^23 * 2^28)
-    const int64_t off = (int64_t)(((1ull << 54) / p + 1) * p);
+    for (int d = 0; d < 7; d++) w[d] = wts[prime][d];
+    const int64_t off = offs[prime];
     const uint32_t mg = (uint32_t)cbi * TC_M + m;
     uint32_t *o = out + ((uint64_t)prime * zc + zl) * N * L.combos + mg;
     const uint32_t zero8[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -249,11 +251,11 @@ __device__ __forceinline__ void drain_quarter(uint32_t lane_addr, int N, int c0,
 //   limbs[prime][z][stage][8-row group][digit][N/8][8 n][8 rows]  (fp16)
 __global__ void __launch_bounds__(256) k_tc_limbs(const QDesc *__restrict__ qd, int nq, int rows, int N,
                                                   uint8_t *__restrict__ limbs) {
-    const uint64_t total = (uint64_t)N * D * (rows / 8);
-    for (uint64_t idx = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; idx < total;
-         idx += (uint64_t)gridDim.x * blockDim.x) {
-        const int n = (int)(idx % N);
-        const uint64_t rest = idx / N;
+    // index space N * D * rows / 8 < 2^32: 32-bit index arithmetic
+    const uint32_t total = (uint32_t)N * D * (uint32_t)(rows / 8);
+    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+        const int n = (int)(idx % (uint32_t)N);
+        const uint32_t rest = idx / (uint32_t)N;
         const int z = (int)(rest % D);
         const int rg = (int)(rest / D);
         const int b = n >> 1, k = n & 1;
@@ -296,9 +298,9 @@ __global__ void __launch_bounds__(256) k_tc_limbs(const QDesc *__restrict__ qd, 
 // Units of one launch: both primes, slots [z0, z0 + zc), every combo block;
 // chunk-local index v -> image unit.
 __device__ __forceinline__ uint64_t chunk_unit(const DbLayout &L, int z0, int zc, uint64_t v) {
-    const uint64_t per_prime = (uint64_t)zc * L.ncb;
-    const uint64_t prime = v / per_prime, r = v % per_prime;
-    return (prime * D + z0 + r / L.ncb) * L.ncb + r % L.ncb;
+    const uint32_t per_prime = (uint32_t)zc * (uint32_t)L.ncb, vv = (uint32_t)v;
+    const uint32_t prime = vv / per_prime, r = vv % per_prime;
+    return ((uint64_t)prime * D + z0 + r / (uint32_t)L.ncb) * L.ncb + r % (uint32_t)L.ncb;
 }
 
 __global__ void __launch_bounds__(TC_THREADS, 1) k_db_mul_tc(const uint32_t *__restrict__ db, DbLayout L, int nq,
@@ -332,6 +334,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_db_mul_tc(const uint32_t *__r
         mbar_init(&C.acc_empty, TC_DRAIN);
         mbar_init(&C.drain, 1);
         C.abort = 0;
+        for (int pr = 0; pr < 2; pr++) {
+            const uint32_t p = pr ? QP1 : QP0;
+            uint64_t wd = (1ull << 32) % p;
+            for (int d = 0; d < 7; d++) {
+                C.wts[pr][d] = (int32_t)wd;
+                wd = (wd << 7) % p;
+            }
+            // a multiple of p above the largest |sum| (< 7 * 2^23 * 2^28)
+            C.off[pr] = (int64_t)(((1ull << 54) / p + 1) * p);
+        }
         fence_mbar_init();
     }
     if (warp == 1) {
@@ -450,11 +462,25 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_db_mul_tc(const uint32_t *__r
             tc_fence_before();
             mbar_arrive(&C.acc_empty);
         }
+        // The converters drain their share of unit ui - 1 after converting
+        // the first stage of unit ui: the digit buffers are free as soon as
+        // the accumulators are full, so the next unit's first MMAs do not
+        // wait for the conversion after the drain.
+        uint64_t prev_u = 0;
+        auto drain_unit = [&](uint32_t unit_idx, uint64_t uu) -> bool {
+            const bool ok = mbar_wait_bounded(&C.acc_full, unit_idx & 1, abort);
+            if (!__all_sync(0xffffffffu, ok)) return false;
+            tc_fence_after();
+            drain_quarter(lane_addr, N, c0, L, z0, zc, uu, m, out, C.wts, C.off);
+            tc_fence_before();
+            mbar_arrive(&C.acc_empty);
+            return true;
+        };
         uint32_t G = 0, ui = 0;
         bool stop = false;
         for (uint64_t v = blockIdx.x; v < units && !stop; v += gridDim.x, ui++) {
             const uint64_t u = chunk_unit(L, z0, zc, v);
-            const uint32_t p = (u / ((uint64_t)L.ncb * D)) ? QP1 : QP0;
+            const uint32_t p = ((uint32_t)u / ((uint32_t)L.ncb * D)) ? QP1 : QP0;
             for (int s = 0; s < S; s++, G++) {
                 const int ds = G % TC_ND;
                 bool ok = mbar_wait_bounded(&C.d_full[ds], (G / TC_ND) & 1, abort);
@@ -487,16 +513,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_db_mul_tc(const uint32_t *__r
                 tmem_wait_st();
                 tc_fence_before();
                 mbar_arrive(&C.a_full[h]);
+                if (s == 0 && ui > 0 && !drain_unit(ui - 1, prev_u)) {
+                    stop = true;
+                    break;
+                }
             }
-            if (stop) break;
-            // this unit's share of the drain
-            const bool ok = mbar_wait_bounded(&C.acc_full, ui & 1, abort);
-            if (!__all_sync(0xffffffffu, ok)) break;
-            tc_fence_after();
-            drain_quarter(lane_addr, N, c0, L, z0, zc, u, m, out);
-            tc_fence_before();
-            mbar_arrive(&C.acc_empty);
+            prev_u = u;
         }
+        if (!stop && ui > 0) drain_unit(ui - 1, prev_u);
     } else {
         // -------------------------------------------------------- drain
         const int q4 = warp & 3;             // TMEM lane quarter of this warp
@@ -518,7 +542,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_db_mul_tc(const uint32_t *__r
             const bool ok = mbar_wait_bounded(&C.acc_full, ui & 1, abort);
             if (!__all_sync(0xffffffffu, ok)) break;
             tc_fence_after();
-            drain_quarter(lane_addr, N, c0, L, z0, zc, chunk_unit(L, z0, zc, v), m, out);
+            drain_quarter(lane_addr, N, c0, L, z0, zc, chunk_unit(L, z0, zc, v), m, out, C.wts, C.off);
             tc_fence_before();
             mbar_arrive(&C.acc_empty);
         }

@@ -210,6 +210,53 @@ def test_db_mul_tc_two_passes(gpu):
     assert np.array_equal(ref[39].astype(np.uint32), O.db_mul(db, sels[39], T, nu1, nu2))
 
 
+def test_db_mul_tc_n48_matches_integer_kernels(gpu):
+    """24 queries: one tensor-core pass at N = 48 (selector columns padded to
+    a multiple of 16); equal to the per-query and the integer batch kernels."""
+    T, nu1, nu2, nq = 4, 7, 5, 24
+    rng = np.random.default_rng(13)
+    db = np.empty((T, 1 << nu2, 1 << nu1, 2, D), dtype=np.uint32)
+    db[..., 0, :] = rng.integers(0, O.Q1, size=db[..., 0, :].shape, dtype=np.uint32)
+    db[..., 1, :] = rng.integers(0, O.Q2, size=db[..., 1, :].shape, dtype=np.uint32)
+    sels = np.empty((nq, 1 << nu1, 2, 2, D), dtype=np.uint32)
+    sels[..., 0, :] = rng.integers(0, O.Q1, size=sels[..., 0, :].shape, dtype=np.uint32)
+    sels[..., 1, :] = rng.integers(0, O.Q2, size=sels[..., 1, :].shape, dtype=np.uint32)
+    gpu.load_db_ntt(9, db, nu1, nu2)
+    outs = {}
+    try:
+        for v in (1, 2, 3):
+            gpu.set_db_mul_variant(v)
+            outs[v] = gpu.db_mul_batch(9, sels, T, nu2)
+    finally:
+        gpu.set_db_mul_variant(0)
+        gpu.unload_db(9)
+    assert np.array_equal(outs[3], outs[1]) and np.array_equal(outs[2], outs[1])
+    assert np.array_equal(outs[3][5].astype(np.uint32), O.db_mul(db, sels[5], T, nu1, nu2))
+
+
+def test_db_mul_batch_small_image(gpu_fix):
+    """n = 1, nu2 = 2: 4 combos per block (no tensor-core shape); the integer
+    batch kernel and the per-query kernel equal the oracle for every query."""
+    T, nu1, nu2, nq = 1, 6, 2, 5
+    rng = np.random.default_rng(14)
+    db = np.empty((T, 1 << nu2, 1 << nu1, 2, D), dtype=np.uint32)
+    db[..., 0, :] = _extreme_planes(db[..., 0, :].shape, O.Q1, rng)
+    db[..., 1, :] = _extreme_planes(db[..., 1, :].shape, O.Q2, rng)
+    sels = np.empty((nq, 1 << nu1, 2, 2, D), dtype=np.uint32)
+    sels[..., 0, :] = _extreme_planes(sels[..., 0, :].shape, O.Q1, rng)
+    sels[..., 1, :] = _extreme_planes(sels[..., 1, :].shape, O.Q2, rng)
+    gpu_fix.load_db_ntt(3, db, nu1, nu2)
+    try:
+        for v in (1, 2):
+            gpu_fix.set_db_mul_variant(v)
+            got = gpu_fix.db_mul_batch(3, sels, T, nu2).astype(np.uint32)
+            for q in range(nq):
+                assert np.array_equal(got[q], O.db_mul(db, sels[q], T, nu1, nu2)), (v, q)
+    finally:
+        gpu_fix.set_db_mul_variant(0)
+        gpu_fix.unload_db(3)
+
+
 def test_fold(gpu):
     x = cases.inputs("fold")
     got = gpu.fold(x["cts"], x["V"], x["nu2"])
