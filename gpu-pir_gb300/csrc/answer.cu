@@ -99,7 +99,10 @@ __global__ void k_narrow(const uint64_t *__restrict__ in, uint32_t *__restrict__
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total;
          i += (uint64_t)gridDim.x * blockDim.x) {
         const Prime c = prime_of((int)((i / D) & 1));
-        uint32_t x = (uint32_t)(in[i] % c.p);
+        // any u64 mod p: the high word first (32-bit), then one Montgomery
+        // reduction of a value below p * 2^32
+        const uint64_t v = in[i];
+        const uint32_t x = mod_u64(((uint64_t)((uint32_t)(v >> 32) % c.p) << 32) | (uint32_t)v, c);
         out[i] = to_m ? to_mont(x, c) : x;
     }
 }
@@ -603,12 +606,20 @@ cudaError_t launch_fold_level(const QDesc *qd, int nq, int level, int max_items,
 
 // ----------------------------------------------------------------- pack
 __device__ __forceinline__ uint32_t rescale_q(uint64_t x, int bits_out) {
-    // round(x * 2^bits_out / q) mod 2^bits_out, x read as centred in Z_q
+    // round(x * 2^bits_out / q) mod 2^bits_out, x read as centred in Z_q:
+    // y = floor((a * 2^bits_out + floor(q/2)) / q).  A double estimate
+    // (absolute error below 2^-18) is made exact with 128-bit products, so no
+    // 128-bit division is needed.
     const uint64_t mask = (1ull << bits_out) - 1;
     const bool neg = x >= (QQ + 1) / 2;
     const uint64_t a = neg ? QQ - x : x;
+    constexpr double INV_Q = 1.0 / (double)QQ;
+    uint64_t y = (uint64_t)llrint(ldexp((double)a, bits_out) * INV_Q);
     const unsigned __int128 num = ((unsigned __int128)a << bits_out) + QQ / 2;
-    const uint64_t y = (uint64_t)(num / QQ) & mask;
+    const unsigned __int128 lo = (unsigned __int128)y * QQ;
+    if (lo > num) y--;
+    else if (lo + QQ <= num) y++;
+    y &= mask;
     return (uint32_t)(neg ? ((0 - y) & mask) : y);
 }
 
