@@ -94,6 +94,10 @@ struct Lane {
     uint8_t *h_resp = nullptr;   // pinned responses [cap][response bytes]
     cudaEvent_t ev[6]{};
     cudaEvent_t done = nullptr;
+    // side stream of the Regev->GSW conversion, forked from the expansion
+    // once its GSW-bit outputs are complete and joined before the folds
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     int *d_err = nullptr;
     uint8_t *limbs = nullptr;           // tensor-core multiply workspace: selector digit
     uint64_t limb_bytes = 0;            // tiles, then the chunk output
@@ -288,6 +292,9 @@ int ensure_staging(sp_ctx *c, uint64_t bytes) {
 int lane_init(sp_ctx *c, Lane &L, int cap) {
     L.cap = cap;
     CU(cudaStreamCreateWithFlags(&L.st, cudaStreamNonBlocking));
+    CU(cudaStreamCreateWithFlags(&L.side, cudaStreamNonBlocking));
+    CU(cudaEventCreateWithFlags(&L.fork_ev, cudaEventDisableTiming));
+    CU(cudaEventCreateWithFlags(&L.join_ev, cudaEventDisableTiming));
     for (auto &e : L.ev) CU(cudaEventCreate(&e));
     CU(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming));
     TRY(alloc(c, (void **)&L.d_err, 16));
@@ -338,6 +345,12 @@ void lane_free(sp_ctx *c, Lane &L) {
     for (auto &e : L.ev)
         if (e) cudaEventDestroy(e);
     if (L.done) cudaEventDestroy(L.done);
+    if (L.side) cudaStreamSynchronize(L.side);
+    if (L.fork_ev) cudaEventDestroy(L.fork_ev);
+    if (L.join_ev) cudaEventDestroy(L.join_ev);
+    if (L.side) cudaStreamDestroy(L.side);
+    L.side = nullptr;
+    L.fork_ev = L.join_ev = nullptr;
     if (L.st) cudaStreamDestroy(L.st);
     L.st = nullptr;
 }
@@ -514,11 +527,12 @@ int choose_mul_variant(sp_ctx *c, Lane &L, int db_id, const Db &db, const QDesc 
 int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot) {
     cudaStream_t st = L.st;
     const StageParams &sp = c->sp;
-    int max_g = 0, max_nu2 = 0, max_items = 0;
+    int max_g = 0, max_nu2 = 0, max_items = 0, fork_round = 0;
     for (int i = 0; i < nq; i++) {
         max_g = std::max(max_g, L.h_qd[i].g);
         max_nu2 = std::max(max_nu2, L.h_qd[i].nu2);
         max_items = std::max(max_items, L.h_qd[i].nu2 * sp.t_gsw);
+        fork_round = std::max(fork_round, L.h_qd[i].capture);   // GSW-bit outputs complete after this round
     }
     // first-dimension multiply: consecutive slots of the same database share
     // a launch; variants are chosen (and autotuned) before any capture
@@ -545,17 +559,27 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot)
     auto enqueue = [&](bool capturing) -> cudaError_t {
         const unsigned ev_flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
         cudaError_t e = cudaEventRecordWithFlags(L.ev[0], st, ev_flags);
-        for (int r = 0; r < max_g && !e; r++)
+        for (int r = 0; r < max_g && !e; r++) {
             e = launch_expand_round(L.d_qd, nq, r, 2 << r, sp, c->d_tw, c->d_neg1, &L.split, st);
+            if (!e && r == fork_round) {
+                // the conversion needs only the GSW-bit encodings: run it on
+                // the side stream, overlapping the remaining rounds and the
+                // multiply
+                e = cudaEventRecord(L.fork_ev, st);
+                if (!e) e = cudaStreamWaitEvent(L.side, L.fork_ev, 0);
+                if (!e) e = launch_regev_to_gsw(L.d_qd, nq, max_items, sp, c->d_tw, L.side);
+                if (!e) e = cudaEventRecord(L.join_ev, L.side);
+            }
+        }
         if (!e) e = cudaEventRecordWithFlags(L.ev[1], st, ev_flags);
-        if (!e) e = launch_regev_to_gsw(L.d_qd, nq, max_items, sp, c->d_tw, st);
-        if (!e) e = cudaEventRecordWithFlags(L.ev[2], st, ev_flags);
+        if (!e) e = cudaEventRecordWithFlags(L.ev[2], st, ev_flags);   // conversion: off the critical path
         for (const Group &gr : groups) {
             if (e) break;
             e = launch_mul_variant(L, c->dbs.at(gr.db_id), L.d_qd + gr.begin, gr.count, gr.variant);
         }
         if (!e) e = cudaEventRecordWithFlags(L.ev[3], st, ev_flags);
         if (!e) e = launch_acc_to_raw(L.d_qd, nq, sp.T * (2 << max_nu2), sp, c->d_tw, st);
+        if (!e) e = cudaStreamWaitEvent(st, L.join_ev, 0);   // the folds need the GSW ciphertexts
         for (int lvl = 0; lvl < max_nu2 && !e; lvl++)
             e = launch_fold_level(L.d_qd, nq, lvl, sp.T << (max_nu2 - 1 - lvl), sp, c->d_tw, &L.split, st);
         if (!e) e = cudaEventRecordWithFlags(L.ev[4], st, ev_flags);
