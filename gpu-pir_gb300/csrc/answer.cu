@@ -5,6 +5,7 @@
 // modulo prime g.  Raw (56-bit) values are rebuilt by an inverse CRT of both
 // groups' INTT outputs exchanged through shared memory.
 #include <algorithm>
+#include <utility>
 
 #include "answer.cuh"
 
@@ -16,6 +17,24 @@ constexpr int THREADS = 256;
 // shared memory: 4 twiddle tables + per group 2 transpose buffers
 constexpr int SMEM_WORDS = TW_WORDS + 2 * 2 * D;
 constexpr int SMEM_BYTES = SMEM_WORDS * 4;
+
+// Launch with programmatic stream serialisation when `pdl` (the kernel then
+// calls pdl_wait() before touching its predecessor's data), else normally.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_ex(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool pdl,
+                      Args &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 struct Ctx {
     const uint32_t *tw;   // 4 tables (TW_WORDS words)
@@ -161,7 +180,9 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_expand_round(const QDesc *
     if (Q.stop > 0 && r > Q.stop && (i & 1)) return;
     if (Q.stop > 0 && r == Q.stop && (i & 1) && (i / 2) >= max_bits) return;
     extern __shared__ __align__(16) uint32_t smem[];
-    load_twiddles(smem, tws);
+    pdl_launch_dependents();
+    load_twiddles(smem, tws);   // constant: may overlap the previous round
+    pdl_wait();
     const int gi = threadIdx.x >> 7, g = gi & 1, sub = gi >> 1, t = threadIdx.x & (GROUP - 1), bar = 1 + gi;
     const Prime c = prime_of(g);
     uint32_t *bufs = smem + TW_WORDS;
@@ -302,14 +323,16 @@ cudaError_t launch_expand_round(const QDesc *qd, int nq, int r, int max_out, con
         const int smem = (TW_WORDS + 4 * 2 * D) * 4 + D * 8;
         cudaError_t e = cudaFuncSetAttribute(k_expand_round<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
-        k_expand_round<2><<<dim3(max_out * split, nq), 512, smem, st>>>(qd, r, sp, tw, neg1, split,
-                                                                        scr ? scr->part : nullptr,
-                                                                        scr ? scr->counters : nullptr);
+        e = launch_ex(k_expand_round<2>, dim3(max_out * split, nq), dim3(512), smem, st, r > 0, qd, r, sp, tw, neg1,
+                      split, scr ? scr->part : nullptr, scr ? scr->counters : nullptr);
+        if (e != cudaSuccess) return e;
     } else {
         const int smem = SMEM_BYTES + D * 8;
         cudaError_t e = cudaFuncSetAttribute(k_expand_round<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
-        k_expand_round<1><<<dim3(max_out, nq), THREADS, smem, st>>>(qd, r, sp, tw, neg1, 1, nullptr, nullptr);
+        e = launch_ex(k_expand_round<1>, dim3(max_out, nq), dim3(THREADS), smem, st, r > 0, qd, r, sp, tw, neg1, 1,
+                      (uint32_t *)nullptr, (unsigned int *)nullptr);
+        if (e != cudaSuccess) return e;
     }
     return cudaGetLastError();
 }
@@ -475,7 +498,9 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_fold_level(const QDesc *__
     if (inst >= sp.T) return;
     __shared__ int s_last;
     extern __shared__ __align__(16) uint32_t smem[];
-    load_twiddles(smem, tws);
+    pdl_launch_dependents();
+    load_twiddles(smem, tws);   // constant: may overlap the previous level
+    pdl_wait();
     const int gi = threadIdx.x >> 7, g = gi & 1, sub = gi >> 1, t = threadIdx.x & (GROUP - 1), bar = 1 + gi;
     const Prime c = prime_of(g);
     uint32_t *bufs = smem + TW_WORDS;           // [group][2][D]
@@ -593,32 +618,37 @@ cudaError_t launch_fold_level(const QDesc *qd, int nq, int level, int max_items,
         const int smem = (TW_WORDS + 4 * 2 * D) * 4;
         cudaError_t e = cudaFuncSetAttribute(k_fold_level<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
-        k_fold_level<2><<<dim3(max_items * split, nq), 512, smem, st>>>(qd, level, sp, tw, split,
-                                                                         scr ? scr->part : nullptr,
-                                                                         scr ? scr->counters : nullptr);
+        e = launch_ex(k_fold_level<2>, dim3(max_items * split, nq), dim3(512), smem, st, level > 0, qd, level, sp, tw,
+                      split, scr ? scr->part : nullptr, scr ? scr->counters : nullptr);
+        if (e != cudaSuccess) return e;
     } else {
         cudaError_t e = cudaFuncSetAttribute(k_fold_level<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
         if (e != cudaSuccess) return e;
-        k_fold_level<1><<<dim3(max_items, nq), THREADS, SMEM_BYTES, st>>>(qd, level, sp, tw, 1, nullptr, nullptr);
+        e = launch_ex(k_fold_level<1>, dim3(max_items, nq), dim3(THREADS), (size_t)SMEM_BYTES, st, level > 0, qd, level,
+                      sp, tw, 1, (uint32_t *)nullptr, (unsigned int *)nullptr);
+        if (e != cudaSuccess) return e;
     }
     return cudaGetLastError();
 }
 
 // ----------------------------------------------------------------- pack
+// floor(2^96 / q): floor(2^(64+b) / q) = RESCALE_M32 >> (32 - b) for b <= 32
+constexpr uint64_t RESCALE_M32 = 0x1136db7cb1full;
+static_assert(RESCALE_M32 == (uint64_t)(((unsigned __int128)1 << 96) / QQ), "reciprocal of q");
+
 __device__ __forceinline__ uint32_t rescale_q(uint64_t x, int bits_out) {
-    // round(x * 2^bits_out / q) mod 2^bits_out, x read as centred in Z_q:
-    // y = floor((a * 2^bits_out + floor(q/2)) / q).  A double estimate
-    // (absolute error below 2^-18) is made exact with 128-bit products, so no
-    // 128-bit division is needed.
-    const uint64_t mask = (1ull << bits_out) - 1;
+    // round(x * 2^bits_out / q) mod 2^bits_out (bits_out <= 32), x read as
+    // centred in Z_q: y = floor((a * 2^bits_out + floor(q/2)) / q).  Integer
+    // only (GB300's FP64 rate is a small fraction of its integer rate): the
+    // fixed-point reciprocal gives y or y - 1 or y - 2 (its error times a is
+    // below 2^-8), and the remainder, below 3q < 2^58, is exact in wrapping
+    // 64-bit arithmetic.
+    const uint64_t mask = bits_out == 32 ? 0xffffffffull : (1ull << bits_out) - 1;
     const bool neg = x >= (QQ + 1) / 2;
     const uint64_t a = neg ? QQ - x : x;
-    constexpr double INV_Q = 1.0 / (double)QQ;
-    uint64_t y = (uint64_t)llrint(ldexp((double)a, bits_out) * INV_Q);
-    const unsigned __int128 num = ((unsigned __int128)a << bits_out) + QQ / 2;
-    const unsigned __int128 lo = (unsigned __int128)y * QQ;
-    if (lo > num) y--;
-    else if (lo + QQ <= num) y++;
+    uint64_t y = __umul64hi(a, RESCALE_M32 >> (32 - bits_out));
+    const uint64_t rem = (a << bits_out) + QQ / 2 - y * QQ;
+    y += (rem >= QQ) + (rem >= 2 * QQ);
     y &= mask;
     return (uint32_t)(neg ? ((0 - y) & mask) : y);
 }

@@ -294,11 +294,35 @@ __device__ __forceinline__ void ntt_inv(uint32_t (&v)[VPT], const uint2 *__restr
 }
 
 // Copy the four twiddle tables into shared memory (all threads of the CTA).
+// Eight loads are issued before their stores, so a CTA pays about one L2
+// latency per 8 x blockDim 16-byte words instead of one per word.
 __device__ __forceinline__ void load_twiddles(uint32_t *dst, const TwiddleSet *src) {
     const uint4 *s = reinterpret_cast<const uint4 *>(src);
     uint4 *d = reinterpret_cast<uint4 *>(dst);
-    for (int i = threadIdx.x; i < TW_WORDS / 4; i += blockDim.x) d[i] = __ldg(s + i);
+    constexpr int NW = TW_WORDS / 4;
+    for (int i0 = threadIdx.x; i0 < NW; i0 += 8 * blockDim.x) {
+        uint4 v[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const int i = i0 + k * blockDim.x;
+            if (i < NW) v[k] = __ldg(s + i);
+        }
+#pragma unroll
+        for (int k = 0; k < 8; k++) {
+            const int i = i0 + k * blockDim.x;
+            if (i < NW) d[i] = v[k];
+        }
+    }
 }
+
+// Programmatic dependent launch.  A kernel launched with programmatic stream
+// serialisation may start while its predecessor in the stream is still
+// running; it must call pdl_wait() before it reads or writes anything the
+// predecessor touches (the predecessor then has completed and its writes are
+// visible).  pdl_launch_dependents() lets the next such kernel start early.
+// Both are no-ops for a kernel launched the ordinary way.
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 // Slot permutation of the automorphism x -> x^tau in NTT form: the slot z
 // evaluates at psi^(2*brev(z)+1); tau(f) at that point is f at
