@@ -338,29 +338,42 @@ cudaError_t launch_expand_round(const QDesc *qd, int nq, int r, int max_out, con
 }
 
 // --------------------------------------------- DB-multiply output to raw
-__global__ void __launch_bounds__(THREADS) k_acc_to_raw(const QDesc *__restrict__ qd, StageParams sp,
-                                                       const TwiddleSet *__restrict__ tws) {
+// Each CTA converts items blockIdx.x, blockIdx.x + gridDim.x, ... of its
+// query (one polynomial = both primes' planes), so the twiddle tables are
+// loaded once per CTA; the next item's planes are fetched while the current
+// one is transformed.
+__global__ void __launch_bounds__(THREADS, 2) k_acc_to_raw(const QDesc *__restrict__ qd, StageParams sp,
+                                                          const TwiddleSet *__restrict__ tws) {
     const QDesc &Q = qd[blockIdx.y];
-    const int item = blockIdx.x;
-    if (!Q.active || item >= sp.T * (2 << Q.nu2)) return;
+    const int n_items = sp.T * (2 << Q.nu2);
+    if (!Q.active || (int)blockIdx.x >= n_items) return;
     extern __shared__ __align__(16) uint32_t smem[];
     const Ctx x = setup(smem, tws);
-    uint32_t v[VPT];
-    ld16(v, Q.acc + ((size_t)item * 2 + x.g) * D + VPT * x.t);
-    ntt_inv(v, tw_inv(x), x.buf, x.c, x.t, x.bar);
-    uint64_t raw[VPT];
-    exchange_icrt(x, v, raw);
-    uint64_t *o = Q.raw + (size_t)item * D;
+    uint32_t next[VPT];
+    ld16(next, Q.acc + ((size_t)blockIdx.x * 2 + x.g) * D + VPT * x.t);
+    for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
+        uint32_t v[VPT];
 #pragma unroll
-    for (int j = 0; j < VPT; j++)
-        if ((j >> 3) == x.g) o[x.t + GROUP * j] = raw[j];
+        for (int j = 0; j < VPT; j++) v[j] = next[j];
+        if (item + (int)gridDim.x < n_items)
+            ld16(next, Q.acc + ((size_t)(item + gridDim.x) * 2 + x.g) * D + VPT * x.t);
+        ntt_inv(v, tw_inv(x), x.buf, x.c, x.t, x.bar);
+        uint64_t raw[VPT];
+        exchange_icrt(x, v, raw);
+        uint64_t *o = Q.raw + (size_t)item * D;
+#pragma unroll
+        for (int j = 0; j < VPT; j++)
+            if ((j >> 3) == x.g) o[x.t + GROUP * j] = raw[j];
+    }
 }
 
 cudaError_t launch_acc_to_raw(const QDesc *qd, int nq, int max_items, const StageParams &sp,
                               const TwiddleSet *tw, cudaStream_t st) {
     cudaError_t e = cudaFuncSetAttribute(k_acc_to_raw, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     if (e != cudaSuccess) return e;
-    k_acc_to_raw<<<dim3(max_items, nq), THREADS, SMEM_BYTES, st>>>(qd, sp, tw);
+    // two resident CTAs per SM over all queries
+    const int per_query = std::max(1, std::min(max_items, 2 * sm_count() / std::max(1, nq)));
+    k_acc_to_raw<<<dim3(per_query, nq), THREADS, SMEM_BYTES, st>>>(qd, sp, tw);
     return cudaGetLastError();
 }
 
@@ -605,8 +618,10 @@ cudaError_t launch_fold_level(const QDesc *qd, int nq, int level, int max_items,
                               const TwiddleSet *tw, const SplitScratch *scr, cudaStream_t st) {
     const uint64_t total = (uint64_t)max_items * nq;
     const int sms = sm_count();
-    if (total < 2ull * sms) {
-        // few folds: 2 groups per prime split the digits; with scratch, each
+    if (total <= (uint64_t)sms) {
+        // few folds (one CTA per SM): 2 groups per prime split the digits;
+        // above that one 256-thread CTA per fold, two per SM, finishes a
+        // level in one wave up to 2 x SMs folds.  With scratch, each
         // fold also spreads over `split` CTAs while that stays within one CTA
         // per SM (this kernel's footprint), at least one digit transform per
         // group
@@ -702,11 +717,15 @@ __global__ void __launch_bounds__(THREADS, 2) k_pack(const QDesc *__restrict__ q
             for (int j = 0; j < VPT; j++) b[j] = mod_u64(ct[D + x.t + GROUP * j], c);
             ntt_fwd(b, tw_fwd(x), x.buf, c, x.t, x.bar);
 #pragma unroll
-            for (int a = 1; a <= PACK_MAX_N; a++)
-                if (a == 1 + r) {
+            for (int j = 0; j < VPT; j++) b[j] = reduce2(b[j], 2 * c.p);
 #pragma unroll
-                    for (int j = 0; j < VPT; j++) acc[a][j] = reduce2(acc[a][j] + reduce2(b[j], 2 * c.p), 2 * c.p);
-                }
+            for (int a = 1; a <= PACK_MAX_N; a++) {
+                // row 1 of ct r goes to acc[1 + r]: a select, not an index
+                // (an index would move acc to local memory)
+                const uint32_t on = (a == 1 + r) ? 0xffffffffu : 0u;
+#pragma unroll
+                for (int j = 0; j < VPT; j++) acc[a][j] = reduce2(acc[a][j] + (b[j] & on), 2 * c.p);
+            }
         }
     }
     if (split > 1) {
@@ -725,11 +744,12 @@ __global__ void __launch_bounds__(THREADS, 2) k_pack(const QDesc *__restrict__ q
             if (s2 == s) continue;
 #pragma unroll
             for (int a = 0; a <= PACK_MAX_N; a++) {
-                if (a > n) break;
-                uint32_t w[VPT];
-                ld16_l2(w, plane(s2, a));
+                if (a <= n) {
+                    uint32_t w[VPT];
+                    ld16_l2(w, plane(s2, a));
 #pragma unroll
-                for (int j = 0; j < VPT; j++) acc[a][j] = reduce2(acc[a][j] + w[j], 2 * c.p);
+                    for (int j = 0; j < VPT; j++) acc[a][j] = reduce2(acc[a][j] + w[j], 2 * c.p);
+                }
             }
         }
         if (threadIdx.x == 0) counters[item] = 0;   // ready for the next launch
