@@ -488,9 +488,23 @@ def run_suite(args) -> None:
         ms16 = g.time_staged(16, 2)
         ok16 = all(np.array_equal(key_sets8[0].decode(g.fetch_response(s)), recs["8GiB"][idx]) for s in range(16))
         peak, _ = measured_peaks()
+        # arithmetic-intensity crossover of the first-dimension multiply: time
+        # per query of each variant as B grows (B queries share one image
+        # pass; 0.5 multiply-add per image byte per query)
+        macs_q = (1 << 20) * 4 * 2048 * 2 * 2
+        per_q_bytes = 512 * 2048 * 16 + 4 * 2048 * 4 * 2048 * 4
+        crossover = []
+        for variant, bs in ((1, (1,)), (2, (2, 4, 8, 16)), (3, (2, 4, 8, 16))):   # batched variants need B >= 2
+            g.set_db_mul_variant(variant)
+            for B in bs:
+                ms = g.time_db_mul(3, B, 2)
+                crossover.append({"variant": variant, "B": B, "ms": ms, "ms_per_query": ms / B,
+                                  "gbs": (img + B * per_q_bytes) / ms / 1e6, "tmacs": B * macs_q / ms / 1e9})
+        g.set_db_mul_variant(0)
         out["db_8gib"] = {"t_exp_right": 16, "load_s": load_s, "decoded_ok": ok, "single_ms": ms1, "single_qps": 1e3 / ms1,
                           "db_mul_ms": mul, "db_mul_gbs": abytes / mul / 1e6, "db_mul_frac": abytes / mul / 1e6 / peak,
-                          "B16_ms": ms16, "B16_qps": 16e3 / ms16, "B16_decoded_ok": ok16}
+                          "B16_ms": ms16, "B16_qps": 16e3 / ms16, "B16_decoded_ok": ok16,
+                          "db_mul_crossover": crossover}
         print(json.dumps({"suite": "db_8gib", **out["db_8gib"]}), flush=True)
         g.close()
 

@@ -92,6 +92,8 @@ struct Lane {
     QDesc *d_qd = nullptr;       // [cap]
     QDesc *h_qd = nullptr;       // pinned mirror
     uint8_t *h_resp = nullptr;   // pinned responses [cap][response bytes]
+    uint64_t *h_query = nullptr; // pinned query staging [cap][2 rows][2 primes][D]
+    int *h_err = nullptr;        // pinned copy of d_err
     cudaEvent_t ev[6]{};
     cudaEvent_t done = nullptr;
     // side stream of the Regev->GSW conversion, forked from the expansion
@@ -302,6 +304,9 @@ int lane_init(sp_ctx *c, Lane &L, int cap) {
     CU(cudaMallocHost(&L.h_qd, sizeof(QDesc) * cap));
     memset(L.h_qd, 0, sizeof(QDesc) * cap);
     CU(cudaMallocHost(&L.h_resp, response_bytes(c->sp) * cap));
+    CU(cudaMallocHost(&L.h_query, 4ull * D * 8 * cap));
+    CU(cudaMallocHost(&L.h_err, 16));
+    *L.h_err = 0;
     CU(cudaMemset(L.d_err, 0, 16));
     // split scratch: partial sums for up to 4 CTAs per SM, 4096 counters
     L.split.slots = 4 * sm_count();
@@ -340,8 +345,12 @@ void lane_free(sp_ctx *c, Lane &L) {
     L.d_qd = nullptr;
     if (L.h_qd) cudaFreeHost(L.h_qd);
     if (L.h_resp) cudaFreeHost(L.h_resp);
+    if (L.h_query) cudaFreeHost(L.h_query);
+    if (L.h_err) cudaFreeHost(L.h_err);
     L.h_qd = nullptr;
     L.h_resp = nullptr;
+    L.h_query = nullptr;
+    L.h_err = nullptr;
     for (auto &e : L.ev)
         if (e) cudaEventDestroy(e);
     if (L.done) cudaEventDestroy(L.done);
@@ -514,7 +523,9 @@ int choose_mul_variant(sp_ctx *c, Lane &L, int db_id, const Db &db, const QDesc 
 }
 
 // Run the answer pipeline for queries in slots [0, nq) (descriptors already
-// in L.h_qd / L.d_qd, queries in slot.query32).  Records stage events.
+// in L.h_qd / L.d_qd, queries in slot.query32).  With `io` the pipeline also
+// downloads the responses to L.h_resp and the error flag to L.h_err (part of
+// the captured graph).  Records stage events.
 //
 // The launches depend only on the batch plan: query count, the largest
 // expansion depth / fold depth / conversion size, and per run of slots on one
@@ -524,7 +535,7 @@ int choose_mul_variant(sp_ctx *c, Lane &L, int db_id, const Db &db, const QDesc 
 // replay saves) and replayed afterwards; per-query inputs reach the kernels
 // through the descriptor array, which is uploaded before each run.  A lane
 // keeps at most 256 graphs; further plans run as plain launches.
-int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot) {
+int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot, bool io) {
     cudaStream_t st = L.st;
     const StageParams &sp = c->sp;
     int max_g = 0, max_nu2 = 0, max_items = 0, fork_round = 0;
@@ -540,7 +551,7 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot)
         int db_id, begin, count, variant;
     };
     std::vector<Group> groups;
-    std::vector<int64_t> key = {nq, max_g, max_nu2, max_items};
+    std::vector<int64_t> key = {nq, max_g, max_nu2, max_items, io ? 1 : 0};
     uint64_t mul_bytes = 0;
     for (int i = 0; i < nq;) {
         int j = i;
@@ -586,6 +597,12 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot)
         if (!e) e = launch_pack(L.d_qd, nq, sp, c->d_tw, &L.split, st);
         if (!e) e = launch_bitpack(L.d_qd, nq, sp, response_bytes(sp), st);
         if (!e) e = cudaEventRecordWithFlags(L.ev[5], st, ev_flags);
+        if (io) {
+            const uint64_t rb = response_bytes(sp);
+            for (int k = 0; k < nq && !e; k++)
+                e = cudaMemcpyAsync(L.h_resp + k * rb, L.slots[k].q.resp, rb, cudaMemcpyDeviceToHost, st);
+            if (!e) e = cudaMemcpyAsync(L.h_err, L.d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
+        }
         return e;
     };
     auto it = L.graphs.find(key);
@@ -641,15 +658,22 @@ int collect_stats(sp_ctx *c, Lane &L) {
     return SP_OK;
 }
 
-int check_device_err(sp_ctx *c, Lane &L) {
-    int h = 0;
-    CU(cudaMemcpyAsync(&h, L.d_err, sizeof(int), cudaMemcpyDeviceToHost, L.st));
-    CU(cudaStreamSynchronize(L.st));
+// The device error flag as last copied to L.h_err (the copy has completed):
+// a bounded wait that ran out is reported once and the flag cleared.
+int take_device_err(sp_ctx *c, Lane &L) {
+    const int h = *L.h_err;
     if (h) {
+        *L.h_err = 0;
         CU(cudaMemsetAsync(L.d_err, 0, sizeof(int), L.st));
         return fail(SP_ERR_DEVICE, "a device-side bounded wait ran out (code " + std::to_string(h) + ")");
     }
     return SP_OK;
+}
+
+int check_device_err(sp_ctx *c, Lane &L) {
+    CU(cudaMemcpyAsync(L.h_err, L.d_err, sizeof(int), cudaMemcpyDeviceToHost, L.st));
+    CU(cudaStreamSynchronize(L.st));
+    return take_device_err(c, L);
 }
 
 // Temporary device buffer for stage calls (freed on scope exit).
@@ -1102,7 +1126,10 @@ static int prepare(sp_ctx *c, Lane &L, int n, sp_request *reqs, std::vector<int>
         sl.db = r.db_id;
         L.h_qd[k] = sl.q;
         db_of_slot[k] = r.db_id;
-        CU(cudaMemcpyAsync(sl.query64, r.query, 4ull * D * 8, cudaMemcpyHostToDevice, L.st));
+        // through the lane's pinned staging, so the upload is asynchronous
+        uint64_t *hq = L.h_query + (uint64_t)k * 4 * D;
+        memcpy(hq, r.query, 4ull * D * 8);
+        CU(cudaMemcpyAsync(sl.query64, hq, 4ull * D * 8, cudaMemcpyHostToDevice, L.st));
         CU(launch_narrow(sl.query64, sl.query32, 4, false, L.st));   // 2 rows x 2 primes
     }
     CU(cudaMemcpyAsync(L.d_qd, L.h_qd, sizeof(QDesc) * n, cudaMemcpyHostToDevice, L.st));
@@ -1115,13 +1142,14 @@ int sp_answer_batch(sp_ctx *c, int32_t count, sp_request *reqs) {
     Lane &L = c->main;
     std::vector<int> order, dbs;
     int rc = prepare(c, L, count, reqs, order, dbs);
-    if (!rc) rc = run_pipeline(c, L, count, dbs);
+    if (!rc) rc = run_pipeline(c, L, count, dbs, true);
     const uint64_t rb = response_bytes(c->sp);
-    for (int k = 0; k < count && !rc; k++) {
-        cudaError_t e = cudaMemcpyAsync(L.h_resp + k * rb, L.slots[k].q.resp, rb, cudaMemcpyDeviceToHost, L.st);
-        if (e != cudaSuccess) rc = fail(SP_ERR_CUDA, std::string("response copy: ") + cudaGetErrorString(e));
-    }
-    if (!rc) rc = check_device_err(c, L);
+    // one synchronisation: the pipeline ends with the copies of the responses
+    // and of the error flag (also after a failure, so that nothing still
+    // reads the staging buffers)
+    const cudaError_t se = cudaStreamSynchronize(L.st);
+    if (!rc && se != cudaSuccess) rc = fail(SP_ERR_CUDA, std::string("answer: ") + cudaGetErrorString(se));
+    if (!rc) rc = take_device_err(c, L);
     if (!rc) {
         for (int k = 0; k < count; k++) memcpy(reqs[order[k]].response, L.h_resp + k * rb, rb);
         rc = collect_stats(c, L);
@@ -1174,7 +1202,7 @@ int sp_run_staged(sp_ctx *c, int32_t count) {
     }
     for (int k = 1; k < count; k++)
         if (dbs[k] < dbs[k - 1]) return fail(SP_ERR_INVALID, "stage slots in database order");
-    TRY(run_pipeline(c, L, count, dbs));
+    TRY(run_pipeline(c, L, count, dbs, false));
     TRY(check_device_err(c, L));
     return collect_stats(c, L);
 }
@@ -1192,7 +1220,7 @@ int sp_time_staged(sp_ctx *c, int32_t count, int32_t iters, double *ms_per_run) 
     int rc = SP_OK;
     float tot = 0;
     if (cudaEventRecord(a, L.st) != cudaSuccess) rc = fail(SP_ERR_CUDA, "event record failed");
-    for (int i = 0; i < iters && !rc; i++) rc = run_pipeline(c, L, count, dbs);
+    for (int i = 0; i < iters && !rc; i++) rc = run_pipeline(c, L, count, dbs, false);
     if (!rc && cudaEventRecord(b, L.st) != cudaSuccess) rc = fail(SP_ERR_CUDA, "event record failed");
     if (!rc) rc = check_device_err(c, L);
     if (!rc && cudaEventElapsedTime(&tot, a, b) != cudaSuccess) rc = fail(SP_ERR_CUDA, "event time failed");
@@ -1594,7 +1622,7 @@ void complete(sp_ctx *c, uint64_t ticket, int status) {
 }
 
 void finish_lane(sp_ctx *c, Lane &L) {
-    int status = check_device_err(c, L);
+    int status = take_device_err(c, L);   // copied by the pipeline before `done`
     if (!status) status = collect_stats(c, L);
     const uint64_t rb = response_bytes(c->sp);
     for (size_t k = 0; k < L.tickets.size(); k++) {
@@ -1637,11 +1665,7 @@ void launch_lane(sp_ctx *c, Lane &L) {
                              batch[k].response_len, 0};
     std::vector<int> order, dbs;
     int rc = prepare(c, L, (int)reqs.size(), reqs.data(), order, dbs);
-    if (!rc) rc = run_pipeline(c, L, (int)reqs.size(), dbs);
-    const uint64_t rb = response_bytes(c->sp);
-    for (size_t k = 0; k < reqs.size() && !rc; k++)
-        if (cudaMemcpyAsync(L.h_resp + k * rb, L.slots[k].q.resp, rb, cudaMemcpyDeviceToHost, L.st) != cudaSuccess)
-            rc = fail(SP_ERR_CUDA, "response copy failed");
+    if (!rc) rc = run_pipeline(c, L, (int)reqs.size(), dbs, true);
     if (!rc && cudaEventRecord(L.done, L.st) != cudaSuccess) rc = fail(SP_ERR_CUDA, "event record failed");
     if (rc) {
         cudaStreamSynchronize(L.st);
