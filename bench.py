@@ -3,11 +3,12 @@
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gpu|reference]
 
 Workload: the plain single-query answer against a 1 GiB database (n = 2,
-p = 256, nu1 = 9, nu2 = 8: 2^17 records of 8 KiB, an 8 GiB CRT-NTT image
+p = 256, nu1 = 9, nu2 = 8: 2^17 records of 8 KiB, a 7 GiB CRT-NTT image
 on the device), d = 2048, q = 268369921 * 249561089, t_exp = 8, t_gsw = 7,
 t_conv = 4.  A step answers one query.  Synthetic seeded data: uniform u8
 records, a seeded client (discrete Gaussian secret, sigma 6.4) and a query
-for a seeded random record.  The database image (8 GiB) is larger than L2,
+for a seeded random record.  The database image (7 GiB: two 28-bit residues
+per coefficient) is larger than L2,
 so every step streams it from HBM.
 
 Printed as one JSON line (rank 0):
@@ -40,10 +41,10 @@ import numpy as np  # noqa: E402
 
 METRIC = "1GiB DB single-query answers/s (Spiral PIR, GPU)"
 UNIT = "queries/s"
-WORKLOAD = {"workload": "spiral-answer-1gib", "db_plain_bytes": 1 << 30, "db_device_bytes": 8 << 30,
+WORKLOAD = {"workload": "spiral-answer-1gib", "db_plain_bytes": 1 << 30, "db_device_bytes": 7 << 30,
             "records": 1 << 17, "record_bytes": 8192, "n": 2, "p": 256, "nu1": 9, "nu2": 8,
             "d": 2048, "t_exp": 8, "t_gsw": 7, "t_conv": 4, "batch": 1,
-            "l2": "database image (8 GiB) larger than L2 (129 MB); no flush needed"}
+            "l2": "database image (7 GiB) larger than L2 (129 MB); no flush needed"}
 THROTTLE = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown", 0x20: "sw_thermal_slowdown",
             0x4: "sw_power_cap", 0x80: "hw_power_brake_slowdown", 0x1: "gpu_idle",
             0x2: "applications_clocks_setting", 0x100: "display_clock_setting"}
@@ -320,7 +321,10 @@ def run_gpu(args, rank, world, local):
         gpu2.close()
 
     value = batch * 1e3 / ms * world
-    algo_bytes = sh.num_records * p.T * 2048 * 8 + (sh.rows * 2048 * 16 + p.T * sh.cols * 4 * 2048 * 4) * batch
+    # image: two 28-bit residues (7 bytes) per plaintext coefficient; selectors
+    # (2 rows x 2 primes x u32 per row and slot) and outputs (2 rows x 2
+    # primes x u32 per combo and slot) of each query
+    algo_bytes = sh.num_records * p.T * 2048 * 7 + (sh.rows * 2048 * 16 + p.T * sh.cols * 4 * 2048 * 4) * batch
     peak, peak_kind = measured_peaks()
     achieved = algo_bytes / (mul_ms / 1e3) / 1e9
     traffic = ncu_traffic()
@@ -466,7 +470,7 @@ def run_suite(args) -> None:
     print(json.dumps({"suite": "uneven_batches", "single": single, "uneven_batches": uneven}), flush=True)
     g.close()
 
-    # 8 GiB database: 2^20 records, 64 GiB device image
+    # 8 GiB database: 2^20 records, 56 GiB device image
     if not args.skip_8gib:
         g = SpiralGPU(p8, max_batch=16)
         g.set_client_keys(0, keys8[0])
@@ -480,7 +484,7 @@ def run_suite(args) -> None:
         g.time_staged(1, 1)
         ms1 = g.time_staged(1, 3)
         mul = g.time_db_mul(3, 1, 3)
-        img = (1 << 20) * 4 * 2048 * 8
+        img = (1 << 20) * 4 * 2048 * 7   # packed image: 7 bytes per coefficient (two 28-bit residues)
         abytes = img + 512 * 2048 * 16 + 4 * 2048 * 4 * 2048 * 4
         for s in range(16):
             g.stage_query(s, 0, 3, q)

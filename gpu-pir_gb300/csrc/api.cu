@@ -561,7 +561,7 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
         TRY(choose_mul_variant(c, L, db_of_slot[i], db, L.d_qd + i, j - i, &variant));
         groups.push_back({db_of_slot[i], i, j - i, variant});
         key.insert(key.end(), {db_of_slot[i], j - i, variant});
-        mul_bytes += db.L.words * 8 + (uint64_t)(j - i) * ((uint64_t)db.L.rows * D * 16 +
+        mul_bytes += db.L.image_bytes() + (uint64_t)(j - i) * ((uint64_t)db.L.rows * D * 16 +
                                                           (uint64_t)db.L.T * db.L.cols * 4 * D * 4);
         i = j;
     }
@@ -797,9 +797,10 @@ static int db_check_shape(sp_ctx *c, int nu1, int nu2) {
         return fail(SP_ERR_UNSUPPORTED, "t_gsw*nu2 GSW-bit encodings do not fit the odd expansion outputs "
                                         "(needs 2^nu1 >= t_gsw*nu2)");
     DbLayout L = make_db_layout(c->sp.T, nu1, nu2);
-    // an image unit (rows x combo block) must be a whole number of 16-byte
-    // copy granules
-    if ((uint64_t)L.rows * L.cb < 4) return fail(SP_ERR_UNSUPPORTED, "database smaller than 4 residues per unit");
+    // an image unit (rows packed rows of cbp 28-bit places) must be a whole
+    // number of 16-byte copy granules
+    if ((uint64_t)L.rows * L.cbp < 32)
+        return fail(SP_ERR_UNSUPPORTED, "database unit smaller than 32 residue places (2^nu1 * combo block < 32)");
     return SP_OK;
 }
 
@@ -812,7 +813,7 @@ static int db_alloc(sp_ctx *c, int db_id, int nu1, int nu2, Db &db) {
         c->dbs.erase(db_id);
     }
     db.L = make_db_layout(c->sp.T, nu1, nu2);
-    db.bytes = db.L.words * 8;
+    db.bytes = db.L.image_bytes();
     return alloc(c, (void **)&db.d, db.bytes);
 }
 
@@ -823,11 +824,15 @@ int sp_db_load_plain(sp_ctx *c, int32_t db_id, const uint8_t *records, uint64_t 
     if (n_records != (1ull << (nu1 + nu2))) return fail(SP_ERR_INVALID, "n_records must be 2^(nu1+nu2)");
     Db db;
     TRY(db_alloc(c, db_id, nu1, nu2, db));
-    // stream the records through a pinned staging buffer in chunks
+    // stream the records through a pinned staging buffer in chunks of whole
+    // packed groups (multiples of 8 records); each chunk is transformed into
+    // `ntt` and packed into the image
     const uint64_t rec_bytes = (uint64_t)c->sp.T * D;
-    const uint64_t chunk_recs = std::max<uint64_t>(1, (64ull << 20) / rec_bytes);
-    Tmp dev(c);
+    const uint64_t chunk_recs =
+        std::min<uint64_t>(n_records, std::max<uint64_t>(8, (4ull << 20) / rec_bytes / 8 * 8));
+    Tmp dev(c), ntt(c);
     int rc = dev.get(2 * chunk_recs * rec_bytes);
+    if (!rc) rc = ntt.get(chunk_recs * c->sp.T * 2 * D * 4);
     if (!rc) rc = ensure_staging(c, 2 * chunk_recs * rec_bytes);
     if (rc) {
         release(c, db.d, db.bytes);
@@ -847,7 +852,8 @@ int sp_db_load_plain(sp_ctx *c, int32_t db_id, const uint8_t *records, uint64_t 
         cudaEventSynchronize(done[buf]);   // staging half free again
         memcpy(hs, records + r0 * rec_bytes, cnt * rec_bytes);
         err = cudaMemcpyAsync(ds, hs, cnt * rec_bytes, cudaMemcpyHostToDevice, c->st);
-        if (err == cudaSuccess) err = launch_db_encode(ds, r0, cnt, c->sp.pt_bits, db.L, db.d, c->d_tw, c->st);
+        if (err == cudaSuccess)
+            err = launch_db_encode(ds, r0, cnt, c->sp.pt_bits, db.L, ntt.as<uint32_t>(), db.d, c->d_tw, c->st);
         cudaEventRecord(done[buf], c->st);
     }
     if (err == cudaSuccess) err = cudaStreamSynchronize(c->st);
@@ -889,7 +895,7 @@ namespace {
 struct ImageHeader {
     char magic[8];          // "SPIRDB1"
     uint32_t version;       // 1
-    uint32_t layout;        // 1: u32 residues [prime][z][combo block][row][combo]
+    uint32_t layout;        // 2: 28-bit residues, 8 per 7 words, [prime][z][combo block][row][combo]
     int32_t n, pt_bits, nu1, nu2;
     uint32_t d, q1, q2;
     uint32_t reserved;
@@ -936,7 +942,7 @@ int sp_db_save(sp_ctx *c, int32_t db_id, const char *path) {
     ImageHeader h{};
     memcpy(h.magic, IMAGE_MAGIC, 8);
     h.version = 1;
-    h.layout = 1;
+    h.layout = 2;
     h.n = c->sp.n;
     h.pt_bits = c->sp.pt_bits;
     h.nu1 = db.L.nu1;
@@ -969,12 +975,12 @@ int sp_db_restore(sp_ctx *c, int32_t db_id, const char *path) {
     if (!in.f) return fail(SP_ERR_IO, std::string("cannot open ") + path);
     ImageHeader h{};
     if (fread(&h, sizeof h, 1, in.f) != 1 || memcmp(h.magic, IMAGE_MAGIC, 8) != 0 || h.version != 1 ||
-        h.layout != 1)
+        h.layout != 2)
         return fail(SP_ERR_INVALID, std::string(path) + " is not a database image of this library");
     if (h.d != (uint32_t)D || h.q1 != QP0 || h.q2 != QP1 || h.n != c->sp.n || h.pt_bits != c->sp.pt_bits)
         return fail(SP_ERR_INVALID, "database image was written for other ring or plaintext parameters");
     const DbLayout L = make_db_layout(c->sp.T, h.nu1, h.nu2);
-    if (h.nu1 < 1 || h.nu2 < 1 || h.nu1 > 14 || h.nu2 > 14 || h.image_bytes != L.words * 8)
+    if (h.nu1 < 1 || h.nu2 < 1 || h.nu1 > 14 || h.nu2 > 14 || h.image_bytes != L.image_bytes())
         return fail(SP_ERR_INVALID, "database image header does not describe a valid shape");
     Db db;
     TRY(db_alloc(c, db_id, h.nu1, h.nu2, db));

@@ -18,7 +18,7 @@
 // instruction; N = 2B rounded up to 16, at most 64, selector columns):
 //  * A = database digits, 128 combos x 16 rows per K-step, in tensor memory:
 //    lane = combo, 8 columns of fp16 pairs (rows 2c, 2c+1) per digit.  The
-//    converter warps write them with tcgen05.st from the u32 image rows that
+//    converter warps write them with tcgen05.st from the packed image rows that
 //    the producer stages in shared memory; two K-step buffers of 32 columns;
 //  * B = the four selector digits side by side, 4N columns (digit j in
 //    columns jN .. jN+N-1), prepared once per batch by k_tc_limbs in the
@@ -59,10 +59,12 @@ namespace {
 constexpr int TC_M = 128;
 constexpr int TC_KC = 32;                     // rows per stage (two K-steps)
 constexpr int TC_NS = 6;                      // selector (B) stages
-constexpr int TC_ND = 6;                      // image (u32) stages
+constexpr int TC_ND = 6;                      // image stages (packed rows)
 constexpr int TC_MAX_N = 2 * TC_MAX_Q;        // 64
 constexpr uint32_t S_STAGE_MAX = 4 * TC_KC * TC_MAX_N * 2;   // 16 KiB
-constexpr uint32_t D_STAGE_BYTES = TC_KC * TC_M * 4;         // 16 KiB
+constexpr uint32_t D_STAGE_BYTES = TC_KC * TC_M * 4;         // 16 KiB slot
+constexpr int TC_RW = TC_M / 8 * 7;                          // words per packed row (112)
+constexpr uint32_t D_COPY_BYTES = TC_KC * TC_RW * 4;         // 14 KiB of packed rows per stage
 constexpr uint32_t S_RING = 0;
 constexpr uint32_t D_RING = S_RING + TC_NS * S_STAGE_MAX;    // 96 KiB
 constexpr uint32_t CTRL = D_RING + TC_ND * D_STAGE_BYTES;    // 192 KiB
@@ -387,9 +389,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_db_mul_tc(const uint32_t *__r
                         stop = true;
                         break;
                     }
-                    mbar_expect_tx(&C.d_full[ds], D_STAGE_BYTES);
-                    tma_bulk_g2s(smem_tc + D_RING + ds * D_STAGE_BYTES, db_src + (uint64_t)s * TC_KC * TC_M,
-                                 D_STAGE_BYTES, &C.d_full[ds]);
+                    mbar_expect_tx(&C.d_full[ds], D_COPY_BYTES);
+                    tma_bulk_g2s(smem_tc + D_RING + ds * D_STAGE_BYTES, db_src + (uint64_t)s * TC_KC * TC_RW,
+                                 D_COPY_BYTES, &C.d_full[ds]);
                 }
             }
             if (stop) {
@@ -447,7 +449,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_db_mul_tc(const uint32_t *__r
         // h = 0 converts rows 0..15 of each stage (K-step 0), h = 1 rows 16..31
         const int q4 = warp & 3, h = (warp - 2) >> 2;
         const int m = q4 * 32 + lane;
-        const uint32_t lds_off = (h * 16 * TC_M + m) * 4;
+        const uint32_t lds_off = h * 16 * TC_RW * 4;   // this parity's first packed row
         const uint32_t ta0 = tmem + ((uint32_t)(q4 * 32) << 16) + TMEM_A + 32 * h;
         const uint32_t lane_addr = tmem + ((uint32_t)(q4 * 32) << 16);
         const int c0 = h * 8;                 // drain chunks h, h + 4, ...
@@ -491,7 +493,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_db_mul_tc(const uint32_t *__r
                 const uint32_t *xs = reinterpret_cast<const uint32_t *>(smem_tc + D_RING + ds * D_STAGE_BYTES + lds_off);
                 uint32_t xr[16];
 #pragma unroll
-                for (int j = 0; j < 16; j++) xr[j] = biased(xs[j * TC_M], p);
+                for (int j = 0; j < 16; j++) xr[j] = biased(unpack1(xs + j * TC_RW, m), p);
                 mbar_arrive(&C.d_empty[ds]);
                 uint32_t w[4][8];     // [digit][row pair]
 #pragma unroll

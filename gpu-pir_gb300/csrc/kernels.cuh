@@ -8,15 +8,22 @@
 
 namespace sp {
 
-// Device layout of one database image: one u32 residue per (prime, combo,
-// row, slot), where combo m = t*cols + col enumerates the n*n plaintext
-// polynomials of every column:
+// Device layout of one database image: one 28-bit residue per (prime,
+// combo, row, slot), where combo m = t*cols + col enumerates the n*n
+// plaintext polynomials of every column:
 //   [prime][z][combo block][row][combo in block]
 // A block holds cb = min(128, combos) combos.  Each (prime, z, block) triple
-// ("unit") is one contiguous stream of rows*cb residues: the first-dimension
+// ("unit") is one contiguous stream of `rows` packed rows: the first-dimension
 // multiply for one slot and prime is the matrix product of that rows x cb
 // block with the query selectors of the slot, so a unit is also exactly the
 // operand tile of the tensor-core multiply (128 combos x rows).
+//
+// Both primes are below 2^28, so a row packs every 8 consecutive combos'
+// residues into 7 words (bits 28j .. 28j+27 of the group's 224-bit
+// little-endian string hold combo 8k+j): 7/8 of the bytes of u32 residues,
+// which is what the HBM-bound one-query multiply reads per query.  A row has
+// cbp = cb rounded up to 8 combo places (the tail of a row narrower than 8
+// combos is zero).
 struct DbLayout {
     int T;        // n*n
     int nu1, nu2;
@@ -24,13 +31,49 @@ struct DbLayout {
     int combos;   // T*cols
     int cb;       // combos per block
     int ncb;      // combos / cb
-    uint64_t words;  // u64 words (two residues each) = rows*combos*D
+    int cbp;      // combo places per packed row (cb rounded up to 8)
+    int rw;       // u32 words per packed row (cbp * 7 / 8)
+    uint64_t words;  // residue pairs (u64 words of the NTT-form planes) = rows*combos*D
     __host__ __device__ uint64_t units() const { return 2ull * D * ncb; }
-    __host__ __device__ uint64_t unit_words32() const { return (uint64_t)rows * cb; }
-    __host__ __device__ uint64_t offset32(int prime, int m, int row, int z) const {
-        return ((((uint64_t)prime * D + z) * ncb + m / cb) * rows + row) * cb + (m % cb);
+    __host__ __device__ uint64_t unit_words32() const { return (uint64_t)rows * rw; }
+    __host__ __device__ uint64_t image_bytes() const { return units() * unit_words32() * 4; }
+    // first word of (prime, z, block, row)
+    __host__ __device__ uint64_t row_offset32(int prime, int z, int block, int row) const {
+        return ((((uint64_t)prime * D + z) * ncb + block) * rows + row) * rw;
     }
 };
+
+constexpr uint32_t RES_MASK = 0x0fffffffu;   // one 28-bit residue
+
+// The 8 residues of one packed group (7 words).
+__device__ __forceinline__ void unpack8(const uint32_t (&w)[7], uint32_t (&r)[8]) {
+    r[0] = w[0] & RES_MASK;
+    r[1] = __funnelshift_r(w[0], w[1], 28) & RES_MASK;
+    r[2] = __funnelshift_r(w[1], w[2], 24) & RES_MASK;
+    r[3] = __funnelshift_r(w[2], w[3], 20) & RES_MASK;
+    r[4] = __funnelshift_r(w[3], w[4], 16) & RES_MASK;
+    r[5] = __funnelshift_r(w[4], w[5], 12) & RES_MASK;
+    r[6] = __funnelshift_r(w[5], w[6], 8) & RES_MASK;
+    r[7] = w[6] >> 4;
+}
+
+__host__ __device__ __forceinline__ void pack8(const uint32_t (&r)[8], uint32_t (&w)[7]) {
+    w[0] = r[0] | r[1] << 28;
+    w[1] = r[1] >> 4 | r[2] << 24;
+    w[2] = r[2] >> 8 | r[3] << 20;
+    w[3] = r[3] >> 12 | r[4] << 16;
+    w[4] = r[4] >> 16 | r[5] << 12;
+    w[5] = r[5] >> 20 | r[6] << 8;
+    w[6] = r[6] >> 24 | r[7] << 4;
+}
+
+// Residue m of a packed row (reads the second word only where the residue
+// straddles two words, so never past the row).
+__device__ __forceinline__ uint32_t unpack1(const uint32_t *row, int m) {
+    const int bit = 28 * m, w = bit >> 5, sh = bit & 31;
+    const uint32_t hi = sh > 4 ? row[w + 1] : 0u;
+    return __funnelshift_r(row[w], hi, sh) & RES_MASK;
+}
 
 DbLayout make_db_layout(int T, int nu1, int nu2);
 
@@ -83,9 +126,13 @@ cudaError_t launch_ntt_planes(uint32_t *a, int count, bool inverse, const Twiddl
 cudaError_t launch_automorph(const uint64_t *in, uint64_t *out, int count, uint32_t t,
                              cudaStream_t st);
 
-// u8 records [n_rec][T][D] (record = row*cols + col) -> database image
+// u8 records [rec_count][T][D] (record = row*cols + col) -> database image.
+// `tmp` holds the chunk's NTT-form residues (rec_count * T * 2 * D u32).  A
+// packed group (8 combos of a row) comes from 8 consecutive records (cols >= 8)
+// or from one whole row (cols < 8), so rec_begin must be a multiple of 8 and
+// rec_count too unless the chunk ends the database.
 cudaError_t launch_db_encode(const uint8_t *records, uint64_t rec_begin, uint64_t rec_count,
-                             int pt_bits, const DbLayout &L, uint32_t *db, const TwiddleSet *tw,
+                             int pt_bits, const DbLayout &L, uint32_t *tmp, uint32_t *db, const TwiddleSet *tw,
                              cudaStream_t st);
 // NTT-form u32 planes [T][cols][rows][2][D] -> database image
 cudaError_t launch_db_import(const uint32_t *planes, const DbLayout &L, uint32_t *db,

@@ -34,7 +34,8 @@ def test_restore_answers_like_encoded(saved):
     byte-identical responses (public keys are randomised per generation, so
     responses are compared within one context)."""
     p, sh, recs, cl, q, ref, path = saved
-    assert os.path.getsize(path) == 64 + sh.rows * sh.cols * p.n * p.n * 2 * P.D * 4
+    # 64-byte header + image: two 28-bit residues (7 bytes) per coefficient
+    assert os.path.getsize(path) == 64 + sh.rows * sh.cols * p.n * p.n * P.D * 7
     with SpiralGPU(p) as gpu:
         gpu.set_client_keys(1, cl.public_keys(sh.nu1, sh.nu2))
         gpu.load_db(1, recs, sh.nu1, sh.nu2)

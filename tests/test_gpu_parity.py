@@ -387,9 +387,9 @@ def test_errors_are_reported(gpu):
 def test_hbm_budget_admission():
     small = SpiralGPU(_p(), hbm_budget_bytes=64 << 20, max_batch=1)
     try:
-        recs = np.zeros((1 << 10, 4, D), dtype=np.uint8)
+        recs = np.zeros((1 << 11, 4, D), dtype=np.uint8)
         with pytest.raises(SpiralError) as e:
-            small.load_db(1, recs, 7, 3)      # 64 MiB image does not fit the budget
+            small.load_db(1, recs, 7, 4)      # 112 MiB image does not fit the budget
         assert e.value.code == 3
     finally:
         small.close()
