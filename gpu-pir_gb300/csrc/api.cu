@@ -212,39 +212,22 @@ Shape shape_of(const sp_ctx *c, int nu1, int nu2) {
     return s;
 }
 
-uint64_t slot_bytes(const sp_ctx *c, const Shape &s) {
+// Carves a slot's workspace out of `base` (or only measures it, with
+// base == nullptr); returns the bytes used.  One function for both, so the
+// allocation always matches the carving.
+uint64_t slot_layout(const sp_ctx *c, const Shape &s, uint8_t *base, Slot *sl) {
     const uint64_t ct = 4ull * D * 4;   // NTT ciphertext bytes
     const int T = c->sp.T;
-    uint64_t b = 0;
-    auto add = [&](uint64_t x) { b += (x + 255) & ~255ull; };
-    add(ct);                                  // query32
-    add(ct * 2);                              // query64
-    add(ct << s.g);                           // v[0]
-    add(ct << s.g);                           // v[1]
-    add((uint64_t)D * 16 << s.nu1);           // sel
-    add(ct * s.nu2 * c->sp.t_gsw);            // gsw_in
-    add((uint64_t)s.nu2 * 2 * 2 * c->sp.t_gsw * 2 * D * 4);   // gsw
-    add(((uint64_t)T * ct) << s.nu2);         // acc
-    add(((uint64_t)T * 2 * D * 8) << s.nu2);  // raw
-    add((uint64_t)(c->sp.n + 1) * c->sp.n * D * 4);           // ms
-    add(response_bytes(c->sp));               // resp
-    return b;
-}
-
-void carve(sp_ctx *c, Slot &sl, const Shape &s) {
-    uint8_t *p = sl.base;
-    const uint64_t ct = 4ull * D * 4;
-    const int T = c->sp.T;
+    uint64_t off = 0;
     auto take = [&](uint64_t x) {
-        uint8_t *r = p;
-        p += (x + 255) & ~255ull;
+        uint8_t *r = base ? base + off : nullptr;
+        off += (x + 255) & ~255ull;
         return r;
     };
-    sl.query32 = (uint32_t *)take(ct);
-    sl.query64 = (uint64_t *)take(ct * 2);
-    QDesc &q = sl.q;
-    q = QDesc{};
-    q.query = sl.query32;
+    uint32_t *query32 = (uint32_t *)take(ct);
+    uint64_t *query64 = (uint64_t *)take(ct * 2);
+    QDesc q{};
+    q.query = query32;
     q.v[0] = (uint32_t *)take(ct << s.g);
     q.v[1] = (uint32_t *)take(ct << s.g);
     q.sel = (uint32_t *)take((uint64_t)D * 16 << s.nu1);
@@ -254,7 +237,17 @@ void carve(sp_ctx *c, Slot &sl, const Shape &s) {
     q.raw = (uint64_t *)take(((uint64_t)T * 2 * D * 8) << s.nu2);
     q.ms = (uint32_t *)take((uint64_t)(c->sp.n + 1) * c->sp.n * D * 4);
     q.resp = take(response_bytes(c->sp));
+    if (sl) {
+        sl->query32 = query32;
+        sl->query64 = query64;
+        sl->q = q;
+    }
+    return off;
 }
+
+uint64_t slot_bytes(const sp_ctx *c, const Shape &s) { return slot_layout(c, s, nullptr, nullptr); }
+
+void carve(sp_ctx *c, Slot &sl, const Shape &s) { slot_layout(c, s, sl.base, &sl); }
 
 // Make sure there are `count` slots big enough for shape `need`.
 int ensure_slots(sp_ctx *c, Lane &L, const Shape &need, int count) {

@@ -4,21 +4,25 @@
 // product:  out[m][n] = sum_row DB[m][row] * SEL[row][n]  (mod p), with m one
 // of the 128 combos of an image unit, n = 2*query + ciphertext row, and
 // row < 2^nu1.  Residues are < 2^28, so the product is made exact on the
-// fp16 tensor cores by splitting both operands into four signed digits:
-//   x (centred to (-p/2, p/2]) = a0 + a1*2^7 + a2*2^14 + a3*2^21,
-//   a0..a2 in [-64, 63], a3 in [-64, 64]   (all exactly representable in fp16)
-// and accumulating the 16 digit products by weight class d = i + j in seven
-// fp32 accumulators C_d.  Every product is at most 2^12 in magnitude and a
-// class holds at most 4 digit pairs, so |C_d| <= 4 * 512 * 2^12 = 2^23 for up
-// to 512 rows: every partial sum is an integer below 2^24, which fp32 holds
-// exactly.  The epilogue returns sum_d C_d * (2^(7d) mod p) reduced mod p,
-// bit-identical to the integer-pipe multiplies.
+// fp16 tensor cores by splitting both operands into four 7-bit digits: the
+// database residue x (as stored, in [0, 2^28)) into unsigned digits
+//   x = u0 + u1*2^7 + u2*2^14 + u3*2^21,   u_i in [0, 127],
+// the selector s (centred to (-p/2, p/2]) into signed digits
+//   s = a0 + a1*2^7 + a2*2^14 + a3*2^21,   a0..a2 in [-64, 63], a3 in [-64, 64]
+// (all exactly representable in fp16), and accumulating the 16 digit
+// products by weight class d = i + j in seven fp32 accumulators C_d.  Every
+// product is at most 127 * 64 in magnitude and a class holds at most 4 digit
+// pairs, so |C_d| <= 4 * 512 * 127 * 64 < 2^24 for up to 512 rows: every
+// partial sum is an integer that fp32 holds exactly.  The epilogue returns
+// sum_d C_d * (2^(7d) mod p) reduced mod p, bit-identical to the
+// integer-pipe multiplies.
 //
 // Layout of the work (tcgen05, cta_group::1, kind::f16, M = 128, K = 16 per
 // instruction; N = 2B rounded up to 16, at most 64, selector columns):
 //  * A = database digits, 128 combos x 16 rows per K-step, in tensor memory:
 //    lane = combo, 8 columns of fp16 pairs (rows 2c, 2c+1) per digit.  The
-//    converter warps write them with tcgen05.st from the packed image rows that
+//    converter warps write them with tcgen05.st from the packed image rows
+//    (the digits are the residue's bit fields) that
 //    the producer stages in shared memory; two K-step buffers of 32 columns;
 //  * B = the four selector digits side by side, 4N columns (digit j in
 //    columns jN .. jN+N-1), prepared once per batch by k_tc_limbs in the
@@ -75,9 +79,6 @@ constexpr int TC_DRAIN = 512;                 // converter + epilogue threads
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t TMEM_A = 448;              // first column of the A buffers
 constexpr int32_t DIGIT_BIAS = 64 * (1 + 128 + 128 * 128);   // 1056832
-// 64 * (1 + 2^7 + 2^14 + 2^21): with it, all four offset digits are plain
-// bit fields of one non-negative word (bits 0-6, 7-13, 14-20, 21-28).
-constexpr uint32_t DIGIT_BIAS4 = 64u * (1u + 128u + 128u * 128u + 128u * 128u * 128u);   // 135274560
 
 struct Ctrl {
     uint64_t s_full[TC_NS], s_empty[TC_NS];
@@ -112,28 +113,25 @@ __device__ __forceinline__ uint32_t digit_pair(uint32_t ulo, uint32_t uhi) {
     return *reinterpret_cast<uint32_t *>(&h);
 }
 
-// Biased word of a canonical residue: centred value + DIGIT_BIAS4, in
-// [0, 2^29).  Its digit fields are the offset digits of digits4.
-__device__ __forceinline__ uint32_t biased(uint32_t x, uint32_t p) {
-    return x + (x > (p >> 1) ? DIGIT_BIAS4 - p : DIGIT_BIAS4);
-}
 
-__device__ __forceinline__ uint32_t hsub1088(uint32_t w) {
+__device__ __forceinline__ uint32_t hsub1024(uint32_t w) {
     __half2 h = *reinterpret_cast<__half2 *>(&w);
-    h = __hsub2(h, __halves2half2(__ushort_as_half(0x6440), __ushort_as_half(0x6440)));
+    h = __hsub2(h, __halves2half2(__ushort_as_half(0x6400), __ushort_as_half(0x6400)));
     return *reinterpret_cast<uint32_t *>(&h);
 }
 
-// The four fp16 digit pairs (digit l of ya, digit l of yb), l = 0..3, of two
-// biased words, with byte permutes instead of per-digit shifts.
-__device__ __forceinline__ void digit_pairs(uint32_t ya, uint32_t yb, uint32_t (&w)[4]) {
-    const uint32_t t0 = __byte_perm(ya, yb, 0x5410);   // bits 0-15 of each
-    const uint32_t t1 = __byte_perm(ya, yb, 0x6521);   // bits 8-23
-    const uint32_t t2 = __byte_perm(ya, yb, 0x7632);   // bits 16-31
-    w[0] = hsub1088((t0 & 0x007F007Fu) | 0x64006400u);
-    w[1] = hsub1088(((t0 >> 7) & 0x007F007Fu) | 0x64006400u);
-    w[2] = hsub1088(((t1 >> 6) & 0x007F007Fu) | 0x64006400u);
-    w[3] = hsub1088(((t2 >> 5) & 0x00FF00FFu) | 0x64006400u);
+// The four fp16 digit pairs (digit l of xa, digit l of xb), l = 0..3, of two
+// residues < 2^28 (unsigned 7-bit digits), with byte permutes instead of
+// per-digit shifts.  0x6400 | u is the fp16 value 1024 + u; subtracting 1024
+// is exact.
+__device__ __forceinline__ void digit_pairs(uint32_t xa, uint32_t xb, uint32_t (&w)[4]) {
+    const uint32_t t0 = __byte_perm(xa, xb, 0x5410);   // bits 0-15 of each
+    const uint32_t t1 = __byte_perm(xa, xb, 0x6521);   // bits 8-23
+    const uint32_t t2 = __byte_perm(xa, xb, 0x7632);   // bits 16-31
+    w[0] = hsub1024((t0 & 0x007F007Fu) | 0x64006400u);
+    w[1] = hsub1024(((t0 >> 7) & 0x007F007Fu) | 0x64006400u);
+    w[2] = hsub1024(((t1 >> 6) & 0x007F007Fu) | 0x64006400u);
+    w[3] = hsub1024(((t2 >> 5) & 0x007F007Fu) | 0x64006400u);
 }
 
 // tcgen05 shared-memory matrix descriptor, no swizzle.
@@ -198,8 +196,8 @@ __device__ __forceinline__ int32_t f2i_small(uint32_t bits) {
 // (chunks of 8): read C_0..C_6, zero them, and write
 //   sum_d C_d 2^(7d) mod p
 // into the chunk output [prime][z - z0][n][combo].  |C_d| <= (pairs of
-// class d) * 2^21, so classes 0, 1, 5, 6 (at most 2 digit pairs) convert
-// with f2i_small and classes 2, 3, 4 with cvt.
+// class d) * 512 * 127 * 64, so classes 0 and 6 (one digit pair, below 2^22)
+// convert with f2i_small and classes 1 to 5 with cvt.
 __device__ __forceinline__ void drain_quarter(uint32_t lane_addr, int N, int c0, const DbLayout &L, int z0,
                                               int zc, uint64_t u, int m, uint32_t *out, const int32_t (&wts)[2][7],
                                               const int64_t (&offs)[2]) {
@@ -230,11 +228,11 @@ __device__ __forceinline__ void drain_quarter(uint32_t lane_addr, int N, int c0,
         for (int c = 0; c < 8; c++) {
             int64_t sum = off;
             sum += (int64_t)f2i_small(v8[0][c]) * w[0];
-            sum += (int64_t)f2i_small(v8[1][c]) * w[1];
+            sum += (int64_t)__float2int_rn(__uint_as_float(v8[1][c])) * w[1];
             sum += (int64_t)__float2int_rn(__uint_as_float(v8[2][c])) * w[2];
             sum += (int64_t)__float2int_rn(__uint_as_float(v8[3][c])) * w[3];
             sum += (int64_t)__float2int_rn(__uint_as_float(v8[4][c])) * w[4];
-            sum += (int64_t)f2i_small(v8[5][c]) * w[5];
+            sum += (int64_t)__float2int_rn(__uint_as_float(v8[5][c])) * w[5];
             sum += (int64_t)f2i_small(v8[6][c]) * w[6];
             const uint64_t x = (uint64_t)sum;
             const uint64_t t = x + (uint64_t)((uint32_t)x * npinv) * p;
@@ -343,8 +341,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_db_mul_tc(const uint32_t *__r
                 C.wts[pr][d] = (int32_t)wd;
                 wd = (wd << 7) % p;
             }
-            // a multiple of p above the largest |sum| (< 7 * 2^23 * 2^28)
-            C.off[pr] = (int64_t)(((1ull << 54) / p + 1) * p);
+            // a multiple of p above the largest |sum| (< 7 * 2^24 * 2^28)
+            C.off[pr] = (int64_t)(((1ull << 55) / p + 1) * p);
         }
         fence_mbar_init();
     }
@@ -450,6 +448,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_db_mul_tc(const uint32_t *__r
         const int q4 = warp & 3, h = (warp - 2) >> 2;
         const int m = q4 * 32 + lane;
         const uint32_t lds_off = h * 16 * TC_RW * 4;   // this parity's first packed row
+        // this combo's word and bit in a packed row; the pair of words read for
+        // the last combo of a row reaches into the next row or the unused tail
+        // of the stage slot (the stray bits are masked off)
+        const int cw = (28 * m) >> 5, csh = (28 * m) & 31;
         const uint32_t ta0 = tmem + ((uint32_t)(q4 * 32) << 16) + TMEM_A + 32 * h;
         const uint32_t lane_addr = tmem + ((uint32_t)(q4 * 32) << 16);
         const int c0 = h * 8;                 // drain chunks h, h + 4, ...
@@ -482,7 +484,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_db_mul_tc(const uint32_t *__r
         bool stop = false;
         for (uint64_t v = blockIdx.x; v < units && !stop; v += gridDim.x, ui++) {
             const uint64_t u = chunk_unit(L, z0, zc, v);
-            const uint32_t p = ((uint32_t)u / ((uint32_t)L.ncb * D)) ? QP1 : QP0;
             for (int s = 0; s < S; s++, G++) {
                 const int ds = G % TC_ND;
                 bool ok = mbar_wait_bounded(&C.d_full[ds], (G / TC_ND) & 1, abort);
@@ -493,7 +494,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_db_mul_tc(const uint32_t *__r
                 const uint32_t *xs = reinterpret_cast<const uint32_t *>(smem_tc + D_RING + ds * D_STAGE_BYTES + lds_off);
                 uint32_t xr[16];
 #pragma unroll
-                for (int j = 0; j < 16; j++) xr[j] = biased(unpack1(xs + j * TC_RW, m), p);
+                for (int j = 0; j < 16; j++)
+                    xr[j] = __funnelshift_r(xs[j * TC_RW + cw], xs[j * TC_RW + cw + 1], csh) & RES_MASK;
                 mbar_arrive(&C.d_empty[ds]);
                 uint32_t w[4][8];     // [digit][row pair]
 #pragma unroll
