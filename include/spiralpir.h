@@ -105,8 +105,9 @@ int sp_db_load_ntt(sp_ctx *ctx, int32_t db_id, const uint32_t *planes, int32_t n
 int sp_db_unload(sp_ctx *ctx, int32_t db_id);
 /* Checkpoint of an encoded database image (no counterpart in the reference,
  * which has no encoder).  sp_db_save writes a 64-byte header (magic
- * "SPIRDB1", version, layout, n, pt_bits, nu1, nu2, d, q1, q2, image bytes,
- * FNV-1a-64 over the image's 64-bit words) followed by the device image;
+ * "SPIRDB1", version, layout (2: 28-bit residues, 8 per 7 words), n, pt_bits,
+ * nu1, nu2, d, q1, q2, image bytes, FNV-1a-64 over the image's 64-bit words)
+ * followed by the device image;
  * sp_db_restore loads
  * such a file as database `db_id`, skipping the encode.  The file must match
  * the context's n and pt_bits; a short file or a checksum mismatch gives
