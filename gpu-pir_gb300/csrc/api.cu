@@ -249,7 +249,11 @@ uint64_t slot_bytes(const sp_ctx *c, const Shape &s) { return slot_layout(c, s, 
 
 void carve(sp_ctx *c, Slot &sl, const Shape &s) { slot_layout(c, s, sl.base, &sl); }
 
-// Make sure there are `count` slots big enough for shape `need`.
+void clear_graphs(Lane &L);
+
+// Make sure there are `count` slots big enough for shape `need`.  Growing
+// the shape reallocates every slot, which drops the lane's graphs (their
+// input and response copies name slot buffers).
 int ensure_slots(sp_ctx *c, Lane &L, const Shape &need, int count) {
     Shape s = L.slot_shape;
     bool grow = need.nu1 > s.nu1 || need.nu2 > s.nu2 || need.g > s.g;
@@ -258,6 +262,7 @@ int ensure_slots(sp_ctx *c, Lane &L, const Shape &need, int count) {
     s.g = std::max(s.g, need.g);
     if (grow) {
         CU(cudaStreamSynchronize(L.st));
+        clear_graphs(L);
         for (auto &sl : L.slots) release(c, sl.base, sl.bytes);
         L.slots.clear();
         L.staged = 0;
@@ -481,6 +486,14 @@ int time_variant(sp_ctx *c, Lane &L, const Db &db, const QDesc *qd, int nq, int 
     return SP_OK;
 }
 
+// Whether choose_mul_variant answers without timing anything.
+bool mul_choice_known(sp_ctx *c, Lane &L, int db_id, const Db &db, int nq) {
+    if (c->mul_force && variant_available(c, L, db, nq, c->mul_force)) return true;
+    if (nq < 2) return true;
+    auto it = c->mul_choice.find(std::make_pair(db_id, ceil_log2((uint64_t)nq)));
+    return it != c->mul_choice.end() && variant_available(c, L, db, nq, it->second);
+}
+
 int choose_mul_variant(sp_ctx *c, Lane &L, int db_id, const Db &db, const QDesc *qd, int nq, int *variant) {
     if (c->mul_force && variant_available(c, L, db, nq, c->mul_force)) {
         *variant = c->mul_force;
@@ -515,10 +528,25 @@ int choose_mul_variant(sp_ctx *c, Lane &L, int db_id, const Db &db, const QDesc 
     return SP_OK;
 }
 
-// Run the answer pipeline for queries in slots [0, nq) (descriptors already
-// in L.h_qd / L.d_qd, queries in slot.query32).  With `io` the pipeline also
-// downloads the responses to L.h_resp and the error flag to L.h_err (part of
-// the captured graph).  Records stage events.
+// Uploads of an answer's inputs: the queries from the lane's pinned staging,
+// converted to u32 residues, and the descriptors from L.h_qd.
+cudaError_t enqueue_inputs(Lane &L, int nq, cudaStream_t st) {
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < nq && !e; k++) {
+        e = cudaMemcpyAsync(L.slots[k].query64, L.h_query + (uint64_t)k * 4 * D, 4ull * D * 8,
+                            cudaMemcpyHostToDevice, st);
+        if (!e) e = launch_narrow(L.slots[k].query64, L.slots[k].query32, 4, false, st);   // 2 rows x 2 primes
+    }
+    if (!e) e = cudaMemcpyAsync(L.d_qd, L.h_qd, sizeof(QDesc) * nq, cudaMemcpyHostToDevice, st);
+    return e;
+}
+
+// Run the answer pipeline for queries in slots [0, nq) (descriptors in
+// L.h_qd).  Without `io` the queries and descriptors are already on the
+// device (sp_stage_query); with `io` the pipeline itself uploads them from the
+// lane's pinned staging (L.h_query, L.h_qd) and downloads the responses to
+// L.h_resp and the error flag to L.h_err, all inside the captured graph.
+// Records stage events.
 //
 // The launches depend only on the batch plan: query count, the largest
 // expansion depth / fold depth / conversion size, and per run of slots on one
@@ -546,6 +574,18 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
     std::vector<Group> groups;
     std::vector<int64_t> key = {nq, max_g, max_nu2, max_items, io ? 1 : 0};
     uint64_t mul_bytes = 0;
+    if (io) {
+        // the autotuner times multiply launches on the staged descriptors:
+        // upload them first when it will run
+        bool known = true;
+        for (int i = 0; i < nq;) {
+            int j = i;
+            while (j < nq && db_of_slot[j] == db_of_slot[i]) j++;
+            known = known && mul_choice_known(c, L, db_of_slot[i], c->dbs.at(db_of_slot[i]), j - i);
+            i = j;
+        }
+        if (!known) CU(enqueue_inputs(L, nq, st));
+    }
     for (int i = 0; i < nq;) {
         int j = i;
         while (j < nq && db_of_slot[j] == db_of_slot[i]) j++;
@@ -562,7 +602,8 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
     // graph records them too
     auto enqueue = [&](bool capturing) -> cudaError_t {
         const unsigned ev_flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
-        cudaError_t e = cudaEventRecordWithFlags(L.ev[0], st, ev_flags);
+        cudaError_t e = io ? enqueue_inputs(L, nq, st) : cudaSuccess;
+        if (!e) e = cudaEventRecordWithFlags(L.ev[0], st, ev_flags);
         for (int r = 0; r < max_g && !e; r++) {
             e = launch_expand_round(L.d_qd, nq, r, 2 << r, sp, c->d_tw, c->d_neg1, &L.split, st);
             if (!e && r == fork_round) {
@@ -626,7 +667,7 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
     } else {
         CU(enqueue(false));
     }
-    uint64_t launches = (uint64_t)max_g + 1 + 1 + (uint64_t)max_nu2 + 2;
+    uint64_t launches = (uint64_t)max_g + 1 + 1 + (uint64_t)max_nu2 + 2 + (io ? (uint64_t)nq : 0);
     for (const Group &gr : groups) {
         c->stats.db_mul_by_variant[gr.variant - 1]++;
         launches += gr.variant == 3 ? 3 * (uint64_t)((gr.count + TC_MAX_Q - 1) / TC_MAX_Q) : 1;
@@ -1125,13 +1166,9 @@ static int prepare(sp_ctx *c, Lane &L, int n, sp_request *reqs, std::vector<int>
         sl.db = r.db_id;
         L.h_qd[k] = sl.q;
         db_of_slot[k] = r.db_id;
-        // through the lane's pinned staging, so the upload is asynchronous
-        uint64_t *hq = L.h_query + (uint64_t)k * 4 * D;
-        memcpy(hq, r.query, 4ull * D * 8);
-        CU(cudaMemcpyAsync(sl.query64, hq, 4ull * D * 8, cudaMemcpyHostToDevice, L.st));
-        CU(launch_narrow(sl.query64, sl.query32, 4, false, L.st));   // 2 rows x 2 primes
+        // into the lane's pinned staging; the pipeline uploads it
+        memcpy(L.h_query + (uint64_t)k * 4 * D, r.query, 4ull * D * 8);
     }
-    CU(cudaMemcpyAsync(L.d_qd, L.h_qd, sizeof(QDesc) * n, cudaMemcpyHostToDevice, L.st));
     return SP_OK;
 }
 

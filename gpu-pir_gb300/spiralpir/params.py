@@ -63,9 +63,13 @@ class SpiralParams:
         return (bits + 63) // 64 * 8
 
     def db_device_bytes(self, nu1: int, nu2: int) -> int:
-        """Bytes of the CRT-NTT database image on the device (two u32 residues
-        per coefficient)."""
-        return (1 << (nu1 + nu2)) * self.T * D * 8
+        """Bytes of the CRT-NTT database image on the device (two 28-bit
+        residues, 7 bytes, per coefficient; combo blocks narrower than 8 are
+        padded to 8 combo places)."""
+        combos = self.T << nu2
+        cb = min(combos, 128)
+        cbp = (cb + 7) // 8 * 8
+        return 2 * D * (combos // cb) * (1 << nu1) * cbp * 7 // 2
 
 
 @dataclasses.dataclass(frozen=True)
