@@ -234,10 +234,12 @@ def test_db_mul_tc_n48_matches_integer_kernels(gpu):
     assert np.array_equal(outs[3][5].astype(np.uint32), O.db_mul(db, sels[5], T, nu1, nu2))
 
 
-def test_db_mul_batch_small_image(gpu_fix):
-    """n = 1, nu2 = 2: 4 combos per block (no tensor-core shape); the integer
-    batch kernel and the per-query kernel equal the oracle for every query."""
-    T, nu1, nu2, nq = 1, 6, 2, 5
+@pytest.mark.parametrize("nu1, nu2", [(6, 2), (5, 1), (5, 3)])
+def test_db_mul_batch_small_image(gpu_fix, nu1, nu2):
+    """n = 1, 2 to 8 combos per block (no tensor-core shape; a packed row
+    narrower than 8 combos is padded): the integer batch kernel and the
+    per-query kernel equal the oracle for every query."""
+    T, nq = 1, 5
     rng = np.random.default_rng(14)
     db = np.empty((T, 1 << nu2, 1 << nu1, 2, D), dtype=np.uint32)
     db[..., 0, :] = _extreme_planes(db[..., 0, :].shape, O.Q1, rng)
@@ -382,6 +384,16 @@ def test_errors_are_reported(gpu):
     with pytest.raises(SpiralError) as e:
         gpu.load_db(99, np.zeros((10, 4, D), dtype=np.uint8), 3, 3)
     assert e.value.code == 1
+
+
+def test_database_unit_too_small_rejected(gpu_fix):
+    """A unit of the packed image (2^nu1 rows x 8 combo places) must be at
+    least 32 residue places (a whole number of 16-byte copies)."""
+    with pytest.raises(SpiralError) as e:
+        gpu_fix.load_db(77, np.zeros((4, 1, D), dtype=np.uint8), 1, 1)
+    assert e.value.code == 6
+    with pytest.raises(SpiralError):
+        gpu_fix.load_db_ntt(77, np.zeros((1, 2, 2, 2, D), dtype=np.uint32), 1, 1)
 
 
 def test_hbm_budget_admission():

@@ -95,6 +95,26 @@ def test_graphs_dropped_when_database_reloaded():
                     assert np.array_equal(cl.decode(r), recs[i])
 
 
+def test_graphs_dropped_when_slots_grow():
+    """Captured plans copy queries and responses through the lane's slot
+    buffers; a query to a larger database reallocates every slot, after
+    which the small database's plan must be captured again, not replayed."""
+    p = P.PARAMS
+    small, large = P.DbShape(6, 4), P.DbShape(7, 5)
+    cl = C.Client(p, seed=85)
+    with SpiralGPU(p, max_batch=1) as gpu:
+        gpu.set_client_keys(1, cl.public_keys(7, 5))
+        rs = C.random_records(small, p, seed=86)
+        rl = C.random_records(large, p, seed=87)
+        gpu.load_db(1, rs, small.nu1, small.nu2)
+        for i in (1, 2, 3):                   # plain, captured, replayed
+            assert np.array_equal(cl.decode(gpu.answer(1, 1, cl.query(small, i))), rs[i])
+        gpu.load_db(2, rl, large.nu1, large.nu2)
+        assert np.array_equal(cl.decode(gpu.answer(1, 2, cl.query(large, 9))), rl[9])   # slots grow
+        for i in (4, 5, 6):
+            assert np.array_equal(cl.decode(gpu.answer(1, 1, cl.query(small, i))), rs[i])
+
+
 def test_serving_threads_match_alone(world):
     gpu, _, reqs, alone = world
     out = [None] * len(reqs)
