@@ -57,57 +57,136 @@ def dist_info():
     return rank, world, local
 
 
+class _Nvml:
+    """SM clock, maximum SM clock, power and clock-event reasons of one GPU,
+    read through NVML (libnvidia-ml, the library nvidia-smi reads); read-only."""
+
+    def __init__(self, index: int):
+        import ctypes
+        self.ct = ctypes
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        h = ctypes.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(index), ctypes.byref(h)) != 0:
+            raise OSError("no NVML device %d" % index)
+        try:
+            self.reasons_fn = lib.nvmlDeviceGetCurrentClocksEventReasons
+        except AttributeError:
+            self.reasons_fn = lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        self.lib, self.h = lib, h
+
+    def sample(self):
+        ct, lib, h = self.ct, self.lib, self.h
+        sm, mx, mw, rs = ct.c_uint(), ct.c_uint(), ct.c_uint(), ct.c_ulonglong()
+        if (lib.nvmlDeviceGetClockInfo(h, 1, ct.byref(sm)) or lib.nvmlDeviceGetMaxClockInfo(h, 1, ct.byref(mx))
+                or self.reasons_fn(h, ct.byref(rs))):
+            return None
+        power = mw.value / 1e3 if lib.nvmlDeviceGetPowerUsage(h, ct.byref(mw)) == 0 else 0.0
+        return float(sm.value), float(mx.value), power, int(rs.value)
+
+
+def _nvml_index(local: int) -> int:
+    """NVML numbers GPUs by PCI order and ignores CUDA_VISIBLE_DEVICES."""
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")
+    if local < len(vis) and vis[local].strip().isdigit():
+        return int(vis[local])
+    return local
+
+
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 50 ms."""
+    """SM clocks, power and clock-event reasons sampled during the timed
+    regions: NVML every 5 ms in a thread (nvidia-smi every 50 ms where NVML
+    cannot be loaded).  Only samples inside a window() count."""
 
     def __init__(self, index: int):
         self.index = index
-        self.samples = []
+        self.samples = []      # (perf_counter, sm MHz, max sm MHz, W, reasons)
+        self.windows = []
         self.proc = None
         self.thread = None
+        self.source = None
+        self.halt = threading.Event()
 
     def start(self):
-        cmd = ["nvidia-smi", "-i", str(self.index),
-               "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active",
-               "--format=csv,noheader,nounits", "-lms", "50"]
         try:
-            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-        except OSError:
-            self.proc = None
-            return self
-        self.thread = threading.Thread(target=self._read, daemon=True)
+            nv = _Nvml(_nvml_index(self.index))
+            if nv.sample() is None:
+                raise OSError("NVML query failed")
+            self.source = "nvml, 5 ms"
+            self.thread = threading.Thread(target=self._poll, args=(nv,), daemon=True)
+        except (OSError, AttributeError):
+            cmd = ["nvidia-smi", "-i", str(self.index),
+                   "--query-gpu=clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active",
+                   "--format=csv,noheader,nounits", "-lms", "50"]
+            try:
+                self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            except OSError:
+                return self
+            self.source = "nvidia-smi, 50 ms"
+            self.thread = threading.Thread(target=self._read, daemon=True)
         self.thread.start()
+        t_end = time.perf_counter() + 3.0    # the first sample precedes the timed regions
+        while not self.samples and time.perf_counter() < t_end and self.thread.is_alive():
+            time.sleep(0.01)
         return self
+
+    def _poll(self, nv):
+        while not self.halt.is_set():
+            s = nv.sample()
+            if s:
+                self.samples.append((time.perf_counter(),) + s)
+            self.halt.wait(0.005)
 
     def _read(self):
         for line in self.proc.stdout:
             parts = [x.strip() for x in line.split(",")]
             if len(parts) >= 4:
                 try:
-                    self.samples.append((float(parts[0]), float(parts[1]), float(parts[2]), int(parts[3], 16)))
+                    self.samples.append((time.perf_counter(), float(parts[0]), float(parts[1]), float(parts[2]),
+                                         int(parts[3], 16)))
                 except ValueError:
                     pass
 
-    def stop(self) -> dict | None:
-        if not self.proc:
-            return None
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except subprocess.TimeoutExpired:
-            self.proc.kill()
+    class _Window:
+        def __init__(self, owner):
+            self.owner = owner
+
+        def __enter__(self):
+            self.t0 = time.perf_counter()
+
+        def __exit__(self, *a):
+            self.owner.windows.append((self.t0, time.perf_counter()))
+
+    def window(self):
+        return ClockSampler._Window(self)
+
+    def stop(self) -> None:
+        self.halt.set()
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
         if self.thread:
             self.thread.join(timeout=2)
-        if not self.samples:
+
+    def summary(self, windows) -> dict | None:
+        """Median / minimum SM clock, power and reasons over the samples taken
+        inside `windows` (a list of (begin, end) perf_counter pairs)."""
+        inside = [s for s in list(self.samples) if any(a <= s[0] <= b for a, b in windows)]
+        if not inside:
             return None
-        sm = sorted(s[0] for s in self.samples)
+        sm = sorted(s[1] for s in inside)
         reasons = set()
-        for s in self.samples:
+        for s in inside:
             for bit, name in THROTTLE.items():
-                if s[3] & bit and name not in ("gpu_idle",):
+                if s[4] & bit and name != "gpu_idle":
                     reasons.add(name)
-        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": max(s[1] for s in self.samples),
-                "power_w_max": max(s[2] for s in self.samples), "samples": len(self.samples),
+        return {"sm_mhz": sm[len(sm) // 2], "sm_min_mhz": sm[0], "sm_max_mhz": max(s[2] for s in inside),
+                "power_w_max": max(s[3] for s in inside), "samples": len(inside),
+                "timed_s": sum(b - a for a, b in windows), "source": self.source,
                 "reasons": sorted(reasons)}
 
 
@@ -249,6 +328,9 @@ def run_gpu(args, rank, world, local):
         import torch.distributed as dist
         dist.init_process_group("gloo")
         barrier = dist.barrier
+    # clocks are sampled from before the warm-up; samples inside the timed
+    # regions (the staged run, the multiply alone, the end-to-end loop) count
+    clocks = ClockSampler(local).start()
     # warm-up (answers through the public API, then staged runs); answering
     # reuses the slots, so the queries are staged after it
     for i in range(args.warmup):
@@ -259,9 +341,9 @@ def run_gpu(args, rank, world, local):
     # device-resident timed region
     if barrier:
         barrier()
-    clocks = ClockSampler(local).start()
     gpu.stats_reset()
-    ms = gpu.time_staged(batch, args.steps)
+    with clocks.window():
+        ms = gpu.time_staged(batch, args.steps)
     st = gpu.stats()
     launches_per_answer = st["launches"] / max(1, args.steps)
     # per-stage split: CUDA events inside three more staged runs
@@ -270,17 +352,19 @@ def run_gpu(args, rank, world, local):
         gpu.run_staged(batch)
     split = gpu.stats()
     # first-dimension multiply alone (roofline): CUDA events around its launches
-    mul_ms = gpu.time_db_mul(1, batch, max(args.steps, 5))
+    with clocks.window():
+        mul_ms = gpu.time_db_mul(1, batch, max(args.steps, 5))
     # end to end through the public API (host buffers)
     lat = []
     out = np.empty(gpu.response_bytes, dtype=np.uint8)
-    t_e2e = time.perf_counter()
-    for i in range(args.steps):
-        t1 = time.perf_counter()
-        gpu.answer(1, 1, queries[i % len(queries)], out=out)
-        lat.append(time.perf_counter() - t1)
-    e2e_s = time.perf_counter() - t_e2e
-    clk = clocks.stop()
+    with clocks.window():
+        t_e2e = time.perf_counter()
+        for i in range(args.steps):
+            t1 = time.perf_counter()
+            gpu.answer(1, 1, queries[i % len(queries)], out=out)
+            lat.append(time.perf_counter() - t1)
+        e2e_s = time.perf_counter() - t_e2e
+    clk = clocks.summary(clocks.windows)
     if barrier:
         barrier()
     # batched answering (B queries per pipeline run), same database
@@ -295,7 +379,8 @@ def run_gpu(args, rank, world, local):
             for s in range(B):
                 gpu2.stage_query(s, 1, 1, queries[s % len(queries)])
             gpu2.time_staged(B, 2)
-            bms = gpu2.time_staged(B, max(2, args.steps // 4))
+            with clocks.window():
+                bms = gpu2.time_staged(B, max(2, args.steps // 4))
             gpu2.stats_reset()
             gpu2.run_staged(B)
             bsplit = gpu2.stats()
@@ -309,7 +394,8 @@ def run_gpu(args, rank, world, local):
             # tensor-core multiply alone: exact fp16 digit products, 16 per
             # residue product (4 x 4 digits), 2 ciphertext rows, B queries
             gpu2.set_db_mul_variant(3)
-            tc_ms = gpu2.time_db_mul(1, B, 3)
+            with clocks.window():
+                tc_ms = gpu2.time_db_mul(1, B, 3)
             gpu2.set_db_mul_variant(0)
             flops = 2.0 * 16 * 2 * B * (sh.num_records * p.T * 2048 * 2)
             tpeak, tkind = measured_peaks("bf16_tflops")
@@ -317,8 +403,10 @@ def run_gpu(args, rank, world, local):
                                     "achieved": flops / (tc_ms / 1e3) / 1e12, "peak": tpeak, "unit": "TFLOP/s",
                                     "frac": flops / (tc_ms / 1e3) / 1e12 / tpeak, "peak_source": tkind,
                                     "flops_per_launch": flops, "launch_ms": tc_ms}
+            entry["clocks"] = clocks.summary(clocks.windows[-2:])
             batched.append(entry)
         gpu2.close()
+    clocks.stop()
 
     value = batch * 1e3 / ms * world
     # image: two 28-bit residues (7 bytes) per plaintext coefficient; selectors
@@ -362,7 +450,7 @@ def run_gpu(args, rank, world, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--batch", type=int, default=1, help="queries per step (1 = plain single-query path)")
