@@ -287,6 +287,18 @@ def cpu_baseline(threads: int | None = None) -> dict:
                       "instances scaled by 255/7 folds; packing"}
 
 
+def max_over_ranks(values, world: int) -> list:
+    """Element-wise maximum of per-rank figures over all ranks (one gloo
+    all-reduce); the figures themselves when world == 1."""
+    if world == 1:
+        return [float(v) for v in values]
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -436,12 +448,12 @@ def run_gpu(args, rank, world, local):
         line["cpu_baseline"] = cpu_baseline()
     gpu.close()
     if world > 1:
-        import torch
+        # the slowest rank sets the whole job's time
+        ms_max, e2e_max = max_over_ranks([ms, e2e_s], world)
+        line["ms_per_step"] = ms_max / batch
+        line["value"] = batch * 1e3 / ms_max * world
+        line["e2e"]["value"] = args.steps / e2e_max * world
         import torch.distributed as dist
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        line["ms_per_step"] = float(t.item()) / batch
-        line["value"] = batch * 1e3 / float(t.item()) * world
         dist.destroy_process_group()
     if rank == 0:
         print(json.dumps(line), flush=True)
