@@ -89,9 +89,13 @@ __device__ __forceinline__ void mac16(uint32_t (&acc)[VPT], const uint32_t (&v)[
     for (int j = 0; j < VPT; j++) acc[j] = reduce2(acc[j] + mont_mul(v[j], w[j], c.p, c.pinv), 2 * c.p);
 }
 
+// Digits (raw >> shift) & mask (mask below 2^32) from the two 32-bit halves.
 __device__ __forceinline__ void digits(uint32_t (&d)[VPT], const uint64_t (&raw)[VPT], int shift, uint64_t mask) {
 #pragma unroll
-    for (int j = 0; j < VPT; j++) d[j] = (uint32_t)((raw[j] >> shift) & mask);
+    for (int j = 0; j < VPT; j++) {
+        const uint32_t lo = (uint32_t)raw[j], hi = (uint32_t)(raw[j] >> 32);
+        d[j] = (shift < 32 ? __funnelshift_r(lo, hi, shift) : hi >> (shift - 32)) & (uint32_t)mask;
+    }
 }
 
 __device__ __forceinline__ uint32_t to_mont(uint32_t x, const Prime &c) {  // canonical -> canonical Montgomery
@@ -232,7 +236,11 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_expand_round(const QDesc *
     for (int k = s * GP + sub; k < tk; k += GP * split) {
         uint32_t d[VPT];
 #pragma unroll
-        for (int j = 0; j < VPT; j++) d[j] = (uint32_t)((raws[t + GROUP * j] >> (bits * k)) & mask);
+        for (int j = 0; j < VPT; j++) {
+            const uint2 x = reinterpret_cast<const uint2 *>(raws)[t + GROUP * j];
+            const int sh = bits * k;
+            d[j] = (sh < 32 ? __funnelshift_r(x.x, x.y, sh) : x.y >> (sh - 32)) & (uint32_t)mask;
+        }
         ntt_fwd(d, twf, buf, c, t, bar);
         mac16(acc0, d, W + ((size_t)(0 * tk + k) * 2 + g) * D + VPT * t, c);
         mac16(acc1, d, W + ((size_t)(1 * tk + k) * 2 + g) * D + VPT * t, c);
@@ -535,13 +543,32 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_fold_level(const QDesc *__
     for (int pr = s * GP + sub; pr < 2 * tg; pr += GP * split) {
         const int row = pr / tg, k = pr % tg;
         const int sh = bits * k;
+        // digit k of both inputs from 32-bit words: a funnel shift of the two
+        // halves below bit 32, the high half alone above
         uint32_t d[VPT];
+        const uint32_t m32 = (uint32_t)mask;
+        if (sh < 32) {
+            const uint2 *w1 = reinterpret_cast<const uint2 *>(v1 + row * D);
+            const uint2 *w0 = reinterpret_cast<const uint2 *>(v0 + row * D);
 #pragma unroll
-        for (int j = 0; j < VPT; j++) {
-            const int e = t + GROUP * j;
-            const uint32_t a = (uint32_t)((__ldg(v1 + row * D + e) >> sh) & mask);
-            const uint32_t b = (uint32_t)((v0[row * D + e] >> sh) & mask);
-            d[j] = a >= b ? a - b : a + c.p - b;
+            for (int j = 0; j < VPT; j++) {
+                const int e = t + GROUP * j;
+                const uint2 x1 = __ldg(w1 + e), x0 = w0[e];
+                const uint32_t a = __funnelshift_r(x1.x, x1.y, sh) & m32;
+                const uint32_t b = __funnelshift_r(x0.x, x0.y, sh) & m32;
+                d[j] = a >= b ? a - b : a + c.p - b;
+            }
+        } else {
+            const uint32_t *h1 = reinterpret_cast<const uint32_t *>(v1 + row * D) + 1;
+            const uint32_t *h0 = reinterpret_cast<const uint32_t *>(v0 + row * D) + 1;
+            const int s2 = sh - 32;
+#pragma unroll
+            for (int j = 0; j < VPT; j++) {
+                const int e = t + GROUP * j;
+                const uint32_t a = (__ldg(h1 + 2 * e) >> s2) & m32;
+                const uint32_t b = (h0[2 * e] >> s2) & m32;
+                d[j] = a >= b ? a - b : a + c.p - b;
+            }
         }
         ntt_fwd(d, twf, buf, c, t, bar);
         const int col = row + 2 * k;
