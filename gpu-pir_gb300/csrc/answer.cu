@@ -281,6 +281,11 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_expand_round(const QDesc *
     // output rows: row 0 = v.row0 + acc0, row 1 = v.row1 + acc1 + tau(v.row1)
     const int zb = VPT * t;
     const int first = GP == 2 ? sub : 0, last = GP == 2 ? sub : 1;
+    // first-dimension selectors (last round, even outputs): the four planes
+    // (row, prime) are staged in shared memory and written as one 16-byte
+    // slot [row 0 q1, row 0 q2, row 1 q1, row 1 q2] per coefficient
+    const bool to_sel = r == Q.g - 1 && !(i & 1) && (i / 2) < (1 << Q.nu1);
+    if (to_sel) __syncthreads();   // every group is done with its transpose buffers
     for (int row = first; row <= last; row++) {
         const uint32_t *src = ct + (row * 2 + g) * D;
         uint32_t o[VPT];
@@ -305,11 +310,13 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_expand_round(const QDesc *
         if (r + 1 < Q.g) st16(Q.v[(r + 1) & 1] + (size_t)i * 4 * D + (row * 2 + g) * D + zb, o);
         if (r == Q.capture && (i & 1) && (i / 2) < max_bits)
             st16(Q.gsw_in + (size_t)(i / 2) * 4 * D + (row * 2 + g) * D + zb, o);
-        if (r == Q.g - 1 && !(i & 1) && (i / 2) < (1 << Q.nu1)) {
-            uint32_t *sl = Q.sel + (size_t)(i / 2) * D * 4;
-#pragma unroll
-            for (int j = 0; j < VPT; j++) sl[(zb + j) * 4 + row * 2 + g] = o[j];
-        }
+        if (to_sel) st16(bufs + (row * 2 + g) * D + zb, o);
+    }
+    if (to_sel) {
+        __syncthreads();
+        uint4 *sl = reinterpret_cast<uint4 *>(Q.sel + (size_t)(i / 2) * D * 4);
+        for (int z = threadIdx.x; z < D; z += blockDim.x)
+            sl[z] = make_uint4(bufs[z], bufs[D + z], bufs[2 * D + z], bufs[3 * D + z]);
     }
 }
 
