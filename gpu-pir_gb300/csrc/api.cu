@@ -3,6 +3,7 @@
 // and the stage entry points used by the parity tests.
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <condition_variable>
@@ -13,6 +14,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/spiralpir.h"
 #include "answer.cuh"
 #include "ctx_view.h"
@@ -22,6 +25,28 @@ using namespace sp;
 namespace {
 
 thread_local std::string g_err;
+
+// NVTX range around an API call (free when no profiler is attached).
+struct TraceRange {
+    explicit TraceRange(const char *name) { nvtxRangePushA(name); }
+    ~TraceRange() { nvtxRangePop(); }
+    TraceRange(const TraceRange &) = delete;
+    TraceRange &operator=(const TraceRange &) = delete;
+};
+
+// Checked mode (SPIRALPIR_CHECKED=1 when the context is created): every
+// device allocation, and every buffer carved out of a query slot, is followed
+// by a guard region filled with GUARD_FILL; the guards are verified after
+// each synchronous call, so a kernel that writes past a buffer's end is
+// reported (SP_ERR_DEVICE) with the buffer's name.
+constexpr uint64_t GUARD_BYTES = 4096;
+constexpr uint8_t GUARD_FILL = 0xA5;
+
+struct Guard {
+    uint8_t *p;
+    uint64_t bytes;
+    std::string what;
+};
 
 int fail(int code, const std::string &msg) {
     g_err = msg;
@@ -167,21 +192,48 @@ struct sp_ctx {
     std::map<uint64_t, TicketState> tickets;
     uint64_t next_ticket = 1;
     uint64_t served = 0, batches = 0;
+    // checked mode: guard regions by allocation base, and the check's
+    // device list and result word
+    bool checked = false;
+    std::map<uint8_t *, std::vector<Guard>> guards;
+    uint64_t *d_guard_list = nullptr;
+    int guard_list_cap = 0;
+    uint32_t *d_guard_bad = nullptr;
 };
 
 namespace {
 
-int alloc(sp_ctx *c, void **p, uint64_t bytes) {
+// Guard region [p, p + bytes) of allocation `base`, filled now.
+int add_guard(sp_ctx *c, uint8_t *base, uint8_t *p, uint64_t bytes, const std::string &what) {
+    CU(cudaMemset(p, GUARD_FILL, bytes));
+    c->guards[base].push_back(Guard{p, bytes, what});
+    return SP_OK;
+}
+
+// Device memory under the HBM budget (`bytes` counted; the guard region of
+// the checked mode is not).
+int alloc(sp_ctx *c, void **p, uint64_t bytes, const char *what = "device buffer") {
     if (c->budget && c->used + bytes > c->budget)
         return fail(SP_ERR_NOMEM, "HBM budget exceeded: need " + std::to_string(bytes) + " more bytes, " +
                                       std::to_string(c->budget - c->used) + " left");
-    cudaError_t e = cudaMalloc(p, bytes);
+    cudaError_t e = cudaMalloc(p, bytes + (c->checked ? GUARD_BYTES : 0));
     if (e != cudaSuccess) {
         *p = nullptr;
         cudaGetLastError();
         return fail(SP_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
     }
     c->used += bytes;
+    if (c->checked) {
+        uint8_t *b = (uint8_t *)*p;
+        const int rc = add_guard(c, b, b + bytes, GUARD_BYTES, what);
+        if (rc) {
+            cudaFree(*p);
+            *p = nullptr;
+            c->used -= bytes;
+            c->guards.erase(b);
+            return rc;
+        }
+    }
     return SP_OK;
 }
 
@@ -189,7 +241,52 @@ void release(sp_ctx *c, void *p, uint64_t bytes) {
     if (p) {
         cudaFree(p);
         c->used -= bytes;
+        c->guards.erase((uint8_t *)p);
     }
+}
+
+// Checked mode: verify every guard region (waits for the device).
+int verify_guards(sp_ctx *c) {
+    if (!c->checked) return SP_OK;
+    std::vector<uint64_t> list;
+    std::vector<const Guard *> who;
+    for (auto &kv : c->guards)
+        for (const Guard &g : kv.second) {
+            list.push_back((uint64_t)(uintptr_t)g.p);
+            list.push_back(g.bytes);
+            who.push_back(&g);
+        }
+    if (who.empty()) return SP_OK;
+    CU(cudaDeviceSynchronize());
+    if ((int)who.size() > c->guard_list_cap) {
+        if (c->d_guard_list) cudaFree(c->d_guard_list);
+        c->d_guard_list = nullptr;
+        c->guard_list_cap = 0;
+        CU(cudaMalloc(&c->d_guard_list, who.size() * 16));
+        c->guard_list_cap = (int)who.size();
+    }
+    if (!c->d_guard_bad) CU(cudaMalloc(&c->d_guard_bad, sizeof(uint32_t)));
+    CU(cudaMemcpy(c->d_guard_list, list.data(), list.size() * 8, cudaMemcpyHostToDevice));
+    CU(cudaMemset(c->d_guard_bad, 0xff, sizeof(uint32_t)));
+    CU(launch_check_guards(c->d_guard_list, (int)who.size(), GUARD_FILL, c->d_guard_bad, nullptr));
+    uint32_t bad = 0;
+    CU(cudaMemcpy(&bad, c->d_guard_bad, sizeof(uint32_t), cudaMemcpyDeviceToHost));
+    if (bad != 0xffffffffu)
+        return fail(SP_ERR_DEVICE, "device buffer overrun: the guard after " + who[bad]->what + " was overwritten");
+    return SP_OK;
+}
+
+// Checked mode start-up: the check must pass, catch one flipped guard byte,
+// and pass again once the byte is restored.
+int guard_self_test(sp_ctx *c) {
+    if (!c->checked || c->guards.empty()) return SP_OK;
+    TRY(verify_guards(c));
+    const Guard &g = c->guards.begin()->second.front();
+    CU(cudaMemset(g.p + g.bytes / 2, 0, 1));
+    const bool caught = verify_guards(c) == SP_ERR_DEVICE;
+    CU(cudaMemset(g.p + g.bytes / 2, GUARD_FILL, 1));
+    if (!caught) return fail(SP_ERR_DEVICE, "guard self-test: a flipped guard byte was not detected");
+    return verify_guards(c);
 }
 
 int check_params(const sp_params *p) {
@@ -215,28 +312,37 @@ Shape shape_of(const sp_ctx *c, int nu1, int nu2) {
 // Carves a slot's workspace out of `base` (or only measures it, with
 // base == nullptr); returns the bytes used.  One function for both, so the
 // allocation always matches the carving.
-uint64_t slot_layout(const sp_ctx *c, const Shape &s, uint8_t *base, Slot *sl) {
+// In checked mode every piece is followed by a guard gap (its alignment
+// padding plus GUARD_BYTES), listed in `gaps` as (offset, bytes, name).
+struct Gap {
+    uint64_t off, bytes;
+    const char *what;
+};
+
+uint64_t slot_layout(const sp_ctx *c, const Shape &s, uint8_t *base, Slot *sl, std::vector<Gap> *gaps = nullptr) {
     const uint64_t ct = 4ull * D * 4;   // NTT ciphertext bytes
     const int T = c->sp.T;
     uint64_t off = 0;
-    auto take = [&](uint64_t x) {
+    auto take = [&](uint64_t x, const char *what) {
         uint8_t *r = base ? base + off : nullptr;
-        off += (x + 255) & ~255ull;
+        const uint64_t end = off + ((x + 255) & ~255ull) + (c->checked ? GUARD_BYTES : 0);
+        if (c->checked && gaps) gaps->push_back(Gap{off + x, end - off - x, what});
+        off = end;
         return r;
     };
-    uint32_t *query32 = (uint32_t *)take(ct);
-    uint64_t *query64 = (uint64_t *)take(ct * 2);
+    uint32_t *query32 = (uint32_t *)take(ct, "slot query (u32)");
+    uint64_t *query64 = (uint64_t *)take(ct * 2, "slot query (u64)");
     QDesc q{};
     q.query = query32;
-    q.v[0] = (uint32_t *)take(ct << s.g);
-    q.v[1] = (uint32_t *)take(ct << s.g);
-    q.sel = (uint32_t *)take((uint64_t)D * 16 << s.nu1);
-    q.gsw_in = (uint32_t *)take(ct * s.nu2 * c->sp.t_gsw);
-    q.gsw = (uint32_t *)take((uint64_t)s.nu2 * 2 * 2 * c->sp.t_gsw * 2 * D * 4);
-    q.acc = (uint32_t *)take(((uint64_t)T * ct) << s.nu2);
-    q.raw = (uint64_t *)take(((uint64_t)T * 2 * D * 8) << s.nu2);
-    q.ms = (uint32_t *)take((uint64_t)(c->sp.n + 1) * c->sp.n * D * 4);
-    q.resp = take(response_bytes(c->sp));
+    q.v[0] = (uint32_t *)take(ct << s.g, "slot expansion buffer 0");
+    q.v[1] = (uint32_t *)take(ct << s.g, "slot expansion buffer 1");
+    q.sel = (uint32_t *)take((uint64_t)D * 16 << s.nu1, "slot selectors");
+    q.gsw_in = (uint32_t *)take(ct * s.nu2 * c->sp.t_gsw, "slot GSW-bit encodings");
+    q.gsw = (uint32_t *)take((uint64_t)s.nu2 * 2 * 2 * c->sp.t_gsw * 2 * D * 4, "slot GSW ciphertexts");
+    q.acc = (uint32_t *)take(((uint64_t)T * ct) << s.nu2, "slot multiply output");
+    q.raw = (uint64_t *)take(((uint64_t)T * 2 * D * 8) << s.nu2, "slot fold buffer");
+    q.ms = (uint32_t *)take((uint64_t)(c->sp.n + 1) * c->sp.n * D * 4, "slot modulus-switched response");
+    q.resp = take(response_bytes(c->sp), "slot response bytes");
     if (sl) {
         sl->query32 = query32;
         sl->query64 = query64;
@@ -247,7 +353,12 @@ uint64_t slot_layout(const sp_ctx *c, const Shape &s, uint8_t *base, Slot *sl) {
 
 uint64_t slot_bytes(const sp_ctx *c, const Shape &s) { return slot_layout(c, s, nullptr, nullptr); }
 
-void carve(sp_ctx *c, Slot &sl, const Shape &s) { slot_layout(c, s, sl.base, &sl); }
+int carve(sp_ctx *c, Slot &sl, const Shape &s) {
+    std::vector<Gap> gaps;
+    slot_layout(c, s, sl.base, &sl, &gaps);
+    for (const Gap &g : gaps) TRY(add_guard(c, sl.base, sl.base + g.off, g.bytes, g.what));
+    return SP_OK;
+}
 
 void clear_graphs(Lane &L);
 
@@ -271,11 +382,11 @@ int ensure_slots(sp_ctx *c, Lane &L, const Shape &need, int count) {
     const uint64_t b = slot_bytes(c, s);
     while ((int)L.slots.size() < count) {
         Slot sl;
-        int rc = alloc(c, (void **)&sl.base, b);
+        int rc = alloc(c, (void **)&sl.base, b, "query slot");
         if (rc) return rc;
         sl.bytes = b;
-        carve(c, sl, s);
         L.slots.push_back(sl);
+        TRY(carve(c, L.slots.back(), s));
     }
     return SP_OK;
 }
@@ -298,7 +409,7 @@ int lane_init(sp_ctx *c, Lane &L, int cap) {
     for (auto &e : L.ev) CU(cudaEventCreate(&e));
     CU(cudaEventCreateWithFlags(&L.done, cudaEventDisableTiming));
     TRY(alloc(c, (void **)&L.d_err, 16));
-    TRY(alloc(c, (void **)&L.d_qd, sizeof(QDesc) * cap));
+    TRY(alloc(c, (void **)&L.d_qd, sizeof(QDesc) * cap, "query descriptors"));
     CU(cudaMallocHost(&L.h_qd, sizeof(QDesc) * cap));
     memset(L.h_qd, 0, sizeof(QDesc) * cap);
     CU(cudaMallocHost(&L.h_resp, response_bytes(c->sp) * cap));
@@ -310,7 +421,7 @@ int lane_init(sp_ctx *c, Lane &L, int cap) {
     L.split.slots = 4 * sm_count();
     L.split.counter_slots = 4096;
     L.split_bytes = (uint64_t)L.split.slots * 4 * D * 4 + (uint64_t)L.split.counter_slots * 4;
-    TRY(alloc(c, (void **)&L.split.part, L.split_bytes));
+    TRY(alloc(c, (void **)&L.split.part, L.split_bytes, "split partial sums"));
     L.split.counters = reinterpret_cast<uint32_t *>(L.split.part + (uint64_t)L.split.slots * 4 * D);
     CU(cudaMemset(L.split.counters, 0, (uint64_t)L.split.counter_slots * 4));
     return SP_OK;
@@ -423,7 +534,7 @@ bool ensure_limbs(sp_ctx *c, Lane &L, const DbLayout &dl) {
         release(c, L.limbs, L.limb_bytes);
         L.limbs = nullptr;
         L.limb_bytes = 0;
-        if (alloc(c, (void **)&L.limbs, need_l) != SP_OK) {
+        if (alloc(c, (void **)&L.limbs, need_l, "tensor-core selector digits") != SP_OK) {
             g_err.clear();
             return false;
         }
@@ -433,7 +544,7 @@ bool ensure_limbs(sp_ctx *c, Lane &L, const DbLayout &dl) {
         release(c, L.tc_out, L.tc_out_bytes);
         L.tc_out = nullptr;
         L.tc_out_bytes = 0;
-        if (alloc(c, (void **)&L.tc_out, need_o) != SP_OK) {
+        if (alloc(c, (void **)&L.tc_out, need_o, "tensor-core chunk output") != SP_OK) {
             g_err.clear();
             return false;
         }
@@ -701,7 +812,7 @@ int take_device_err(sp_ctx *c, Lane &L) {
         CU(cudaMemsetAsync(L.d_err, 0, sizeof(int), L.st));
         return fail(SP_ERR_DEVICE, "a device-side bounded wait ran out (code " + std::to_string(h) + ")");
     }
-    return SP_OK;
+    return verify_guards(c);
 }
 
 int check_device_err(sp_ctx *c, Lane &L) {
@@ -718,7 +829,7 @@ struct Tmp {
     explicit Tmp(sp_ctx *ctx) : c(ctx) {}
     int get(uint64_t bytes) {
         b = bytes;
-        return alloc(c, &p, bytes ? bytes : 16);
+        return alloc(c, &p, bytes ? bytes : 16, "stage call buffer");
     }
     ~Tmp() { release(c, p, b ? b : 16); }
     template <typename T> T *as() const { return (T *)p; }
@@ -757,6 +868,7 @@ int sp_ctx_create(const sp_params *params, uint64_t hbm_budget_bytes, sp_ctx **o
     c->sp.t_gsw = params->t_gsw;
     c->sp.t_conv = params->t_conv;
     c->budget = hbm_budget_bytes;
+    if (const char *ck = std::getenv("SPIRALPIR_CHECKED")) c->checked = ck[0] && ck[0] != '0';
     auto bail = [&](int rc) {
         sp_ctx_destroy(c);
         return rc;
@@ -766,8 +878,8 @@ int sp_ctx_create(const sp_params *params, uint64_t hbm_budget_bytes, sp_ctx **o
     if (rc) return bail(rc);
     c->st = c->main.st;
     c->d_err = c->main.d_err;
-    rc = alloc(c, (void **)&c->d_tw, sizeof(TwiddleSet));
-    if (!rc) rc = alloc(c, (void **)&c->d_neg1, (uint64_t)LOGD * 2 * D * 4);
+    rc = alloc(c, (void **)&c->d_tw, sizeof(TwiddleSet), "twiddle tables");
+    if (!rc) rc = alloc(c, (void **)&c->d_neg1, (uint64_t)LOGD * 2 * D * 4, "x^-2^r factors");
     if (rc) return bail(rc);
     // constant tables
     std::vector<TwiddleSet> tw(1);
@@ -790,6 +902,8 @@ int sp_ctx_create(const sp_params *params, uint64_t hbm_budget_bytes, sp_ctx **o
     if (cudaMemcpy(c->d_tw, tw.data(), sizeof(TwiddleSet), cudaMemcpyHostToDevice) != cudaSuccess ||
         cudaMemcpy(c->d_neg1, neg1.data(), neg1.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess)
         return bail(fail(SP_ERR_CUDA, "constant upload failed"));
+    rc = guard_self_test(c);
+    if (rc) return bail(rc);
     *out = c;
     return SP_OK;
 }
@@ -804,6 +918,8 @@ int sp_ctx_destroy(sp_ctx *c) {
     release(c, c->d_tw, sizeof(TwiddleSet));
     release(c, c->d_neg1, (uint64_t)LOGD * 2 * D * 4);
     if (c->h_stage) cudaFreeHost(c->h_stage);
+    if (c->d_guard_list) cudaFree(c->d_guard_list);
+    if (c->d_guard_bad) cudaFree(c->d_guard_bad);
     delete c;
     return SP_OK;
 }
@@ -812,6 +928,13 @@ int sp_response_bytes(const sp_ctx *c, uint64_t *bytes) {
     if (!c || !bytes) return fail(SP_ERR_INVALID, "NULL argument");
     *bytes = response_bytes(c->sp);
     return SP_OK;
+}
+
+int sp_check_guards(sp_ctx *c, int32_t *checked) {
+    if (!c || !checked) return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    *checked = c->checked ? 1 : 0;
+    return verify_guards(c);
 }
 
 int sp_hbm_used(const sp_ctx *c, uint64_t *bytes) {
@@ -848,13 +971,14 @@ static int db_alloc(sp_ctx *c, int db_id, int nu1, int nu2, Db &db) {
     }
     db.L = make_db_layout(c->sp.T, nu1, nu2);
     db.bytes = db.L.image_bytes();
-    return alloc(c, (void **)&db.d, db.bytes);
+    return alloc(c, (void **)&db.d, db.bytes, "database image");
 }
 
 int sp_db_load_plain(sp_ctx *c, int32_t db_id, const uint8_t *records, uint64_t n_records, int32_t nu1,
                      int32_t nu2) {
     if (!c || !records) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_db_load_plain");
     if (n_records != (1ull << (nu1 + nu2))) return fail(SP_ERR_INVALID, "n_records must be 2^(nu1+nu2)");
     Db db;
     TRY(db_alloc(c, db_id, nu1, nu2, db));
@@ -904,6 +1028,7 @@ int sp_db_load_plain(sp_ctx *c, int32_t db_id, const uint8_t *records, uint64_t 
 int sp_db_load_ntt(sp_ctx *c, int32_t db_id, const uint32_t *planes, int32_t nu1, int32_t nu2) {
     if (!c || !planes) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_db_load_ntt");
     Db db;
     TRY(db_alloc(c, db_id, nu1, nu2, db));
     Tmp dev(c);
@@ -965,6 +1090,7 @@ constexpr uint64_t CKPT_CHUNK = 64ull << 20;
 int sp_db_save(sp_ctx *c, int32_t db_id, const char *path) {
     if (!c || !path) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_db_save");
     auto it = c->dbs.find(db_id);
     if (it == c->dbs.end()) return fail(SP_ERR_NOT_FOUND, "unknown database id");
     const Db &db = it->second;
@@ -1004,6 +1130,7 @@ int sp_db_save(sp_ctx *c, int32_t db_id, const char *path) {
 int sp_db_restore(sp_ctx *c, int32_t db_id, const char *path) {
     if (!c || !path) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_db_restore");
     File in;
     in.f = fopen(path, "rb");
     if (!in.f) return fail(SP_ERR_IO, std::string("cannot open ") + path);
@@ -1044,6 +1171,7 @@ int sp_db_restore(sp_ctx *c, int32_t db_id, const char *path) {
 int sp_db_unload(sp_ctx *c, int32_t db_id) {
     if (!c) return fail(SP_ERR_INVALID, "NULL context");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_db_unload");
     auto it = c->dbs.find(db_id);
     if (it == c->dbs.end()) return fail(SP_ERR_NOT_FOUND, "unknown database id");
     TRY(sync_all(c));
@@ -1071,6 +1199,7 @@ int sp_client_set_keys(sp_ctx *c, int32_t client_id, const uint64_t *exp_left, i
     if (n_left < 1 || n_left > LOGD || n_right < 1 || n_right > LOGD)
         return fail(SP_ERR_INVALID, "expansion key counts must be in [1, 11]");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_client_set_keys");
     const StageParams &s = c->sp;
     const uint64_t P = 2ull * D;   // words per NTT poly
     const uint64_t wl = (uint64_t)n_left * 2 * s.t_left * P, wr = (uint64_t)n_right * 2 * s.t_right * P;
@@ -1087,7 +1216,7 @@ int sp_client_set_keys(sp_ctx *c, int32_t client_id, const uint64_t *exp_left, i
     cl.n_left = n_left;
     cl.n_right = n_right;
     cl.bytes = words * 4;
-    TRY(alloc(c, (void **)&cl.keys, cl.bytes));
+    TRY(alloc(c, (void **)&cl.keys, cl.bytes, "client keys"));
     Tmp up(c);
     int rc = up.get(words * 8);
     if (rc) {
@@ -1121,6 +1250,7 @@ int sp_client_set_keys(sp_ctx *c, int32_t client_id, const uint64_t *exp_left, i
 int sp_client_evict(sp_ctx *c, int32_t client_id) {
     if (!c) return fail(SP_ERR_INVALID, "NULL context");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_client_evict");
     auto it = c->clients.find(client_id);
     if (it == c->clients.end()) return fail(SP_ERR_NOT_FOUND, "unknown client id");
     TRY(sync_all(c));
@@ -1175,6 +1305,7 @@ static int prepare(sp_ctx *c, Lane &L, int n, sp_request *reqs, std::vector<int>
 int sp_answer_batch(sp_ctx *c, int32_t count, sp_request *reqs) {
     if (!c || !reqs) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_answer_batch");
     Lane &L = c->main;
     std::vector<int> order, dbs;
     int rc = prepare(c, L, count, reqs, order, dbs);
@@ -1204,6 +1335,7 @@ int sp_answer(sp_ctx *c, int32_t client_id, int32_t db_id, const uint64_t *query
 int sp_stage_query(sp_ctx *c, int32_t slot, int32_t client_id, int32_t db_id, const uint64_t *query) {
     if (!c || !query) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_stage_query");
     if (slot < 0 || slot >= c->main.cap) return fail(SP_ERR_INVALID, "slot out of range");
     auto ci = c->clients.find(client_id);
     auto di = c->dbs.find(db_id);
@@ -1228,6 +1360,7 @@ int sp_stage_query(sp_ctx *c, int32_t slot, int32_t client_id, int32_t db_id, co
 int sp_run_staged(sp_ctx *c, int32_t count) {
     if (!c) return fail(SP_ERR_INVALID, "NULL context");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_run_staged");
     Lane &L = c->main;
     if (count < 1 || count > L.staged) return fail(SP_ERR_INVALID, "count exceeds staged queries");
     std::vector<int> dbs(count);
@@ -1246,6 +1379,7 @@ int sp_run_staged(sp_ctx *c, int32_t count) {
 int sp_time_staged(sp_ctx *c, int32_t count, int32_t iters, double *ms_per_run) {
     if (!c || !ms_per_run) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_time_staged");
     Lane &L = c->main;
     if (count < 1 || count > L.staged || iters < 1) return fail(SP_ERR_INVALID, "count/iters out of range");
     std::vector<int> dbs(count);
@@ -1270,6 +1404,7 @@ int sp_time_staged(sp_ctx *c, int32_t count, int32_t iters, double *ms_per_run) 
 int sp_fetch_response(sp_ctx *c, int32_t slot, uint8_t *response, uint64_t response_len) {
     if (!c || !response) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_fetch_response");
     Lane &L = c->main;
     if (slot < 0 || slot >= (int)L.slots.size()) return fail(SP_ERR_INVALID, "slot out of range");
     const uint64_t rb = response_bytes(c->sp);
@@ -1283,6 +1418,7 @@ int sp_set_db_mul_variant(sp_ctx *c, int32_t variant) {
     if (!c) return fail(SP_ERR_INVALID, "NULL context");
     if (variant < 0 || variant > 3) return fail(SP_ERR_INVALID, "variant must be 0 (auto), 1, 2 or 3");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_set_db_mul_variant");
     c->mul_force = variant;
     return SP_OK;
 }
@@ -1290,6 +1426,7 @@ int sp_set_db_mul_variant(sp_ctx *c, int32_t variant) {
 int sp_set_graphs(sp_ctx *c, int32_t on) {
     if (!c) return fail(SP_ERR_INVALID, "NULL context");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_set_graphs");
     c->use_graphs = on != 0;
     return SP_OK;
 }
@@ -1297,6 +1434,7 @@ int sp_set_graphs(sp_ctx *c, int32_t on) {
 int sp_stats(sp_ctx *c, sp_stats_out *out) {
     if (!c || !out) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_stats");
     *out = c->stats;
     return SP_OK;
 }
@@ -1304,6 +1442,7 @@ int sp_stats(sp_ctx *c, sp_stats_out *out) {
 int sp_stats_reset(sp_ctx *c) {
     if (!c) return fail(SP_ERR_INVALID, "NULL context");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_stats_reset");
     c->stats = sp_stats_out{};
     return SP_OK;
 }
@@ -1311,6 +1450,7 @@ int sp_stats_reset(sp_ctx *c) {
 int sp_time_db_mul(sp_ctx *c, int32_t db_id, int32_t nq, int32_t iters, double *ms_per_launch) {
     if (!c || !ms_per_launch) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_time_db_mul");
     Lane &L = c->main;
     auto di = c->dbs.find(db_id);
     if (di == c->dbs.end()) return fail(SP_ERR_NOT_FOUND, "unknown database id");
@@ -1335,6 +1475,7 @@ int sp_time_db_mul(sp_ctx *c, int32_t db_id, int32_t nq, int32_t iters, double *
 int sp_ntt_fwd(sp_ctx *c, const uint64_t *raw, uint64_t *crt, uint64_t count) {
     if (!c || !raw || !crt || !count) return fail(SP_ERR_INVALID, "NULL argument or zero count");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_ntt_fwd");
     Tmp a(c), b(c);
     TRY(a.get(count * D * 8));
     TRY(b.get(count * 2 * D * 8));
@@ -1345,12 +1486,13 @@ int sp_ntt_fwd(sp_ctx *c, const uint64_t *raw, uint64_t *crt, uint64_t count) {
     CU(launch_widen(b.as<uint32_t>(), w.as<uint64_t>(), count * 2, false, c->st));
     CU(cudaMemcpyAsync(crt, w.p, count * 2 * D * 8, cudaMemcpyDeviceToHost, c->st));
     CU(cudaStreamSynchronize(c->st));
-    return SP_OK;
+    return verify_guards(c);
 }
 
 int sp_ntt_inv(sp_ctx *c, const uint64_t *crt, uint64_t *raw, uint64_t count) {
     if (!c || !raw || !crt || !count) return fail(SP_ERR_INVALID, "NULL argument or zero count");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_ntt_inv");
     Tmp a(c), n(c), o(c);
     TRY(a.get(count * 2 * D * 8));
     TRY(n.get(count * 2 * D * 4));
@@ -1360,13 +1502,14 @@ int sp_ntt_inv(sp_ctx *c, const uint64_t *crt, uint64_t *raw, uint64_t count) {
     CU(launch_from_ntt(n.as<uint32_t>(), o.as<uint64_t>(), (int)count, c->d_tw, c->st));
     CU(cudaMemcpyAsync(raw, o.p, count * D * 8, cudaMemcpyDeviceToHost, c->st));
     CU(cudaStreamSynchronize(c->st));
-    return SP_OK;
+    return verify_guards(c);
 }
 
 int sp_automorph(sp_ctx *c, const uint64_t *raw, uint64_t *out, uint64_t count, uint32_t t) {
     if (!c || !raw || !out || !count) return fail(SP_ERR_INVALID, "NULL argument or zero count");
     if (!(t & 1)) return fail(SP_ERR_INVALID, "automorphism exponent must be odd");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_automorph");
     Tmp a(c), b(c);
     TRY(a.get(count * D * 8));
     TRY(b.get(count * D * 8));
@@ -1374,13 +1517,14 @@ int sp_automorph(sp_ctx *c, const uint64_t *raw, uint64_t *out, uint64_t count, 
     CU(launch_automorph(a.as<uint64_t>(), b.as<uint64_t>(), (int)count, t, c->st));
     CU(cudaMemcpyAsync(out, b.p, count * D * 8, cudaMemcpyDeviceToHost, c->st));
     CU(cudaStreamSynchronize(c->st));
-    return SP_OK;
+    return verify_guards(c);
 }
 
 int sp_expand(sp_ctx *c, int32_t client_id, const uint64_t *query, int32_t nu1, int32_t nu2, int32_t rounds,
               uint64_t *out) {
     if (!c || !query || !out) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_expand");
     auto ci = c->clients.find(client_id);
     if (ci == c->clients.end()) return fail(SP_ERR_NOT_FOUND, "unknown client id");
     if (nu1 < 1 || nu2 < 1 || nu1 > 14 || nu2 > 14) return fail(SP_ERR_INVALID, "nu1/nu2 out of range");
@@ -1438,13 +1582,14 @@ int sp_expand(sp_ctx *c, int32_t client_id, const uint64_t *query, int32_t nu1, 
     CU(launch_widen(fin, w.as<uint64_t>(), nout * 4, false, c->st));
     CU(cudaMemcpyAsync(out, w.p, ct * 8 * nout, cudaMemcpyDeviceToHost, c->st));
     CU(cudaStreamSynchronize(c->st));
-    return SP_OK;
+    return verify_guards(c);
 }
 
 int sp_regev_to_gsw(sp_ctx *c, int32_t client_id, const uint64_t *regev, int32_t nu2, uint64_t *gsw) {
     if (!c || !regev || !gsw) return fail(SP_ERR_INVALID, "NULL argument");
     if (nu2 < 1 || nu2 > 14) return fail(SP_ERR_INVALID, "nu2 out of range");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_regev_to_gsw");
     auto ci = c->clients.find(client_id);
     if (ci == c->clients.end()) return fail(SP_ERR_NOT_FOUND, "unknown client id");
     const uint64_t ct = 4ull * D;
@@ -1469,12 +1614,13 @@ int sp_regev_to_gsw(sp_ctx *c, int32_t client_id, const uint64_t *regev, int32_t
     CU(launch_widen(g.as<uint32_t>(), w.as<uint64_t>(), gwords / D, true, c->st));
     CU(cudaMemcpyAsync(gsw, w.p, gwords * 8, cudaMemcpyDeviceToHost, c->st));
     CU(cudaStreamSynchronize(c->st));
-    return SP_OK;
+    return verify_guards(c);
 }
 
 int sp_gsw_neg(sp_ctx *c, const uint64_t *gsw, int32_t count, uint64_t *neg) {
     if (!c || !gsw || !neg || count < 1) return fail(SP_ERR_INVALID, "NULL argument or bad count");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_gsw_neg");
     const uint64_t words = (uint64_t)count * 2 * 2 * c->sp.t_gsw * 2 * D;
     Tmp a(c), b(c), o(c);
     TRY(a.get(words * 8));
@@ -1486,12 +1632,13 @@ int sp_gsw_neg(sp_ctx *c, const uint64_t *gsw, int32_t count, uint64_t *neg) {
     CU(launch_widen(o.as<uint32_t>(), a.as<uint64_t>(), words / D, false, c->st));
     CU(cudaMemcpyAsync(neg, a.p, words * 8, cudaMemcpyDeviceToHost, c->st));
     CU(cudaStreamSynchronize(c->st));
-    return SP_OK;
+    return verify_guards(c);
 }
 
 int sp_db_mul(sp_ctx *c, int32_t db_id, const uint64_t *sel, uint64_t *acc) {
     if (!c || !sel || !acc) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_db_mul");
     auto di = c->dbs.find(db_id);
     if (di == c->dbs.end()) return fail(SP_ERR_NOT_FOUND, "unknown database id");
     const DbLayout &L = di->second.L;
@@ -1523,6 +1670,7 @@ int sp_db_mul_batch(sp_ctx *c, int32_t db_id, int32_t nq, const uint64_t *sel, u
     if (!c || !sel || !acc) return fail(SP_ERR_INVALID, "NULL argument");
     if (nq < 1 || nq > 1024) return fail(SP_ERR_INVALID, "nq must be in [1, 1024]");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_db_mul_batch");
     auto di = c->dbs.find(db_id);
     if (di == c->dbs.end()) return fail(SP_ERR_NOT_FOUND, "unknown database id");
     const Db &db = di->second;
@@ -1564,6 +1712,7 @@ int sp_fold(sp_ctx *c, const uint64_t *cts, const uint64_t *gsw, int32_t T, int3
     if (!c || !cts || !gsw || !out) return fail(SP_ERR_INVALID, "NULL argument");
     if (T < 1 || T > c->sp.T || nu2 < 1 || nu2 > 14) return fail(SP_ERR_INVALID, "T or nu2 out of range");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_fold");
     const uint64_t raw_words = ((uint64_t)T * 2 * D) << nu2;
     const uint64_t gwords = (uint64_t)nu2 * 2 * 2 * c->sp.t_gsw * 2 * D;
     Tmp r(c), g64(c), g(c), qd(c);
@@ -1588,12 +1737,13 @@ int sp_fold(sp_ctx *c, const uint64_t *cts, const uint64_t *gsw, int32_t T, int3
         CU(cudaMemcpyAsync(out + (uint64_t)t * 2 * D, r.as<uint64_t>() + ((uint64_t)t << nu2) * 2 * D, 2ull * D * 8,
                            cudaMemcpyDeviceToHost, c->st));
     CU(cudaStreamSynchronize(c->st));
-    return SP_OK;
+    return verify_guards(c);
 }
 
 int sp_pack(sp_ctx *c, int32_t client_id, const uint64_t *cts, uint8_t *response, uint64_t response_len) {
     if (!c || !cts || !response) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_pack");
     auto ci = c->clients.find(client_id);
     if (ci == c->clients.end()) return fail(SP_ERR_NOT_FOUND, "unknown client id");
     const uint64_t rb = response_bytes(c->sp);
@@ -1617,7 +1767,7 @@ int sp_pack(sp_ctx *c, int32_t client_id, const uint64_t *cts, uint8_t *response
     CU(launch_bitpack(qd.as<QDesc>(), 1, c->sp, rb, c->st));
     CU(cudaMemcpyAsync(response, resp.p, rb, cudaMemcpyDeviceToHost, c->st));
     CU(cudaStreamSynchronize(c->st));
-    return SP_OK;
+    return verify_guards(c);
 }
 
 }  // extern "C"
@@ -1675,6 +1825,7 @@ void finish_lane(sp_ctx *c, Lane &L) {
 
 // Launch up to L.cap queued requests on lane L (lock held).
 void launch_lane(sp_ctx *c, Lane &L) {
+    TraceRange trace_("serve_batch");
     std::vector<Pending> batch;
     while (!c->queue.empty() && (int)batch.size() < L.cap) {
         Pending p = std::move(c->queue.front());
@@ -1752,6 +1903,7 @@ int sp_serve_start(sp_ctx *c, int32_t lanes) {
     if (!c) return fail(SP_ERR_INVALID, "NULL context");
     if (lanes < 1 || lanes > 8) return fail(SP_ERR_INVALID, "lanes must be in [1, 8]");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_serve_start");
     if (c->serving) return fail(SP_ERR_INVALID, "already serving");
     // every lane reserves max_batch workspace slots for the largest loaded
     // database shape now, so admission later only depends on the HBM budget
@@ -1793,6 +1945,7 @@ int sp_serve_stop(sp_ctx *c) {
     if (!c) return fail(SP_ERR_INVALID, "NULL context");
     {
         std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_serve_stop");
         if (!c->serving) return SP_OK;
         c->stopping = true;
     }
@@ -1812,6 +1965,7 @@ int sp_serve_stop(sp_ctx *c) {
 int sp_submit(sp_ctx *c, const sp_request *req, uint64_t *ticket) {
     if (!c || !req || !ticket || !req->query || !req->response) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_submit");
     if (!c->serving || c->stopping) return fail(SP_ERR_INVALID, "serving loop not running (sp_serve_start)");
     if (req->response_len < response_bytes(c->sp)) return fail(SP_ERR_INVALID, "response buffer too small");
     Pending p;
@@ -1834,6 +1988,7 @@ int sp_submit(sp_ctx *c, const sp_request *req, uint64_t *ticket) {
 int sp_poll(sp_ctx *c, uint64_t ticket, int32_t *done, int32_t *status) {
     if (!c || !done || !status) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_poll");
     auto it = c->tickets.find(ticket);
     if (it == c->tickets.end()) return fail(SP_ERR_NOT_FOUND, "unknown ticket");
     *done = it->second.done;
@@ -1863,6 +2018,7 @@ int sp_wait_timed(sp_ctx *c, uint64_t ticket, int32_t *status, double *server_ms
 int sp_serve_stats(sp_ctx *c, uint64_t *served, uint64_t *batches, uint64_t *queued) {
     if (!c || !served || !batches || !queued) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_serve_stats");
     *served = c->served;
     *batches = c->batches;
     *queued = c->queue.size();

@@ -109,6 +109,10 @@ struct StageParams {
 // Multiprocessor count of the current device.
 int sm_count();
 
+// Checked mode: *bad = min(*bad, index of every region (address, length
+// pairs) whose bytes are not all `fill`).
+cudaError_t launch_check_guards(const uint64_t *regions, int n, uint8_t fill, uint32_t *bad, cudaStream_t st);
+
 // Twiddle tables (device, one set per context).
 void build_twiddles_host(TwiddleSet *host);
 

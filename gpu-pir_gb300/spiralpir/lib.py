@@ -101,6 +101,7 @@ _SIGS = {
     "sp_fold": [_P, _P, _P, _I, _I, _P],
     "sp_fold_noalloc": [_P, _P, _P, _I, _I, _P],
     "sp_pack": [_P, _I, _P, _P, _U64],
+    "sp_check_guards": [_P, _P],
 }
 
 
@@ -109,7 +110,7 @@ def exported_symbols() -> list[str]:
 
 
 def load(path: str = LIB_PATH):
-    """Load (building it first if sources are newer) the CUDA library."""
+    """Load the CUDA library, building it first when the shared object is missing."""
     global _lib
     if _lib is not None:
         return _lib
@@ -174,6 +175,14 @@ class SpiralGPU:
             pass
 
     # -- resources ---------------------------------------------------------
+    def check_guards(self) -> bool:
+        """Verify the guard regions now; True when the context runs in
+        checked mode (SPIRALPIR_CHECKED=1 at creation).  Raises SpiralError
+        when a guard was overwritten."""
+        on = _I()
+        _check(self.lib.sp_check_guards(self.h, ctypes.byref(on)))
+        return bool(on.value)
+
     def hbm_used(self) -> int:
         v = _U64()
         _check(self.lib.sp_hbm_used(self.h, ctypes.byref(v)))

@@ -89,6 +89,15 @@ int sp_ctx_destroy(sp_ctx *ctx);
 int sp_last_error(char *buf, size_t len);
 int sp_response_bytes(const sp_ctx *ctx, uint64_t *bytes);
 int sp_hbm_used(const sp_ctx *ctx, uint64_t *bytes);
+/* Checked mode (environment variable SPIRALPIR_CHECKED=1 when the context is
+ * created; no counterpart in the reference): every device allocation, and
+ * every buffer carved out of a query slot, is followed by a guard region of
+ * fill bytes, checked after each synchronous call, so that a kernel writing
+ * past the end of a buffer is reported as SP_ERR_DEVICE naming the buffer.
+ * Context creation verifies that the check catches one flipped guard byte.
+ * sp_check_guards sets *checked (1 in checked mode) and verifies the guards
+ * now (SP_OK when checked mode is off). */
+int sp_check_guards(sp_ctx *ctx, int32_t *checked);
 
 /* ------------------------------------------------------------------ */
 /* Databases.  Record i = row * 2^nu2 + col; a record is n*n plaintext
