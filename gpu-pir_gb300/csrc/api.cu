@@ -930,6 +930,15 @@ int sp_response_bytes(const sp_ctx *c, uint64_t *bytes) {
     return SP_OK;
 }
 
+int sp_wait_probe(sp_ctx *c, int32_t limit_ms) {
+    if (!c) return fail(SP_ERR_INVALID, "NULL context");
+    if (limit_ms < 1 || limit_ms > 1000) return fail(SP_ERR_INVALID, "limit_ms must be in [1, 1000]");
+    std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_wait_probe");
+    CU(launch_wait_probe(c->main.d_err, (uint64_t)limit_ms * 1000000ull, c->main.st));
+    return check_device_err(c, c->main);
+}
+
 int sp_check_guards(sp_ctx *c, int32_t *checked) {
     if (!c || !checked) return fail(SP_ERR_INVALID, "NULL argument");
     std::lock_guard<std::mutex> lk(c->mu);

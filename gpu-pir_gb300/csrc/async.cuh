@@ -56,15 +56,16 @@ __device__ __forceinline__ uint64_t global_ns() {
 constexpr uint64_t WAIT_LIMIT_NS = 1000000000ull;
 
 // Wait for phase `parity` of `bar`.  Gives up (returns false) after
-// WAIT_LIMIT_NS, setting *abort, or as soon as another thread has set *abort.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, volatile int *abort) {
+// limit_ns, setting *abort, or as soon as another thread has set *abort.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, volatile int *abort,
+                                                  uint64_t limit_ns = WAIT_LIMIT_NS) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = global_ns();
     for (uint32_t i = 1;; i++) {
         if (mbar_try_wait(bar, parity)) return true;
         if ((i & 15) == 0) {
             if (*abort) return false;
-            if (global_ns() - t0 > WAIT_LIMIT_NS) {
+            if (global_ns() - t0 > limit_ns) {
                 *abort = 1;
                 return false;
             }

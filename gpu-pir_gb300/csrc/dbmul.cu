@@ -455,4 +455,30 @@ cudaError_t launch_db_mul_batch(const uint32_t *db, const DbLayout &L, const QDe
     return cudaGetLastError();
 }
 
+// ----------------------------------------------------- bounded-wait probe
+// The failure path of the multiply kernels' barrier waits, run on purpose
+// without a GPU fault: every thread waits on an mbarrier whose one expected
+// arrival never comes, with the same bounded wait as the multiply (limit
+// `limit_ns`).  The first thread to give up sets the shared abort flag, the
+// others stop at their next check, and thread 0 sets the error flag the host
+// reads (code 1, as a multiply timeout) before the kernel returns.
+__global__ void k_wait_probe(int *err, uint64_t limit_ns) {
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int abort;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        abort = 0;
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const bool ok = mbar_wait_bounded(&bar, 0, &abort, limit_ns);
+    __syncthreads();
+    if (threadIdx.x == 0 && !ok) atomicExch(err, 1);
+}
+
+cudaError_t launch_wait_probe(int *err, uint64_t limit_ns, cudaStream_t st) {
+    k_wait_probe<<<1, 64, 0, st>>>(err, limit_ns);
+    return cudaGetLastError();
+}
+
 }  // namespace sp

@@ -109,6 +109,10 @@ struct StageParams {
 // Multiprocessor count of the current device.
 int sm_count();
 
+// One CTA whose barrier wait nothing completes: gives up after limit_ns and
+// sets *err = 1 (the failure path of the multiply kernels' bounded waits).
+cudaError_t launch_wait_probe(int *err, uint64_t limit_ns, cudaStream_t st);
+
 // Checked mode: *bad = min(*bad, index of every region (address, length
 // pairs) whose bytes are not all `fill`).
 cudaError_t launch_check_guards(const uint64_t *regions, int n, uint8_t fill, uint32_t *bad, cudaStream_t st);

@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(_HERE, "libspiralpir.so")
 HEADER = os.path.join(os.path.dirname(os.path.dirname(_HERE)), "include", "spiralpir.h")
 
 SP_OK = 0
-ERRORS = {1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "NOT_FOUND", 5: "DEVICE", 6: "UNSUPPORTED"}
+ERRORS = {1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "NOT_FOUND", 5: "DEVICE", 6: "UNSUPPORTED", 7: "IO"}
 
 
 class SpiralError(RuntimeError):
@@ -102,6 +102,7 @@ _SIGS = {
     "sp_fold_noalloc": [_P, _P, _P, _I, _I, _P],
     "sp_pack": [_P, _I, _P, _P, _U64],
     "sp_check_guards": [_P, _P],
+    "sp_wait_probe": [_P, _I],
 }
 
 
@@ -182,6 +183,11 @@ class SpiralGPU:
         on = _I()
         _check(self.lib.sp_check_guards(self.h, ctypes.byref(on)))
         return bool(on.value)
+
+    def wait_probe(self, limit_ms: int) -> None:
+        """Run the bounded-wait failure path once: raises SpiralError
+        (SP_ERR_DEVICE) after about limit_ms; the context stays usable."""
+        _check(self.lib.sp_wait_probe(self.h, limit_ms))
 
     def hbm_used(self) -> int:
         v = _U64()

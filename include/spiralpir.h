@@ -98,6 +98,12 @@ int sp_hbm_used(const sp_ctx *ctx, uint64_t *bytes);
  * sp_check_guards sets *checked (1 in checked mode) and verifies the guards
  * now (SP_OK when checked mode is off). */
 int sp_check_guards(sp_ctx *ctx, int32_t *checked);
+/* Failure-path self-test of the device waits (no counterpart in the
+ * reference): runs one kernel whose barrier wait nothing completes, with the
+ * multiply kernels' bounded wait shortened to limit_ms (1 .. 1000).  The
+ * wait gives up, the kernel sets the device error flag and returns, and the
+ * call returns SP_ERR_DEVICE; the context stays usable.  No GPU fault. */
+int sp_wait_probe(sp_ctx *ctx, int32_t limit_ms);
 
 /* ------------------------------------------------------------------ */
 /* Databases.  Record i = row * 2^nu2 + col; a record is n*n plaintext
