@@ -95,8 +95,8 @@ class DbShape:
 PARAMS = SpiralParams()
 SHAPE_8MIB = DbShape(7, 3)      # 1024 records of 8 KiB: 8 MiB plaintext
 SHAPE_64MIB = DbShape(8, 5)     # 8192 records: 64 MiB plaintext
-SHAPE_1GIB = DbShape(9, 8)      # 2^17 records: 1 GiB plaintext, 8 GiB on device
-SHAPE_8GIB = DbShape(9, 11)     # 2^20 records: 8 GiB plaintext, 64 GiB on device
+SHAPE_1GIB = DbShape(9, 8)      # 2^17 records: 1 GiB plaintext, 7 GiB image on the device
+SHAPE_8GIB = DbShape(9, 11)     # 2^20 records: 8 GiB plaintext, 56 GiB image on the device
 
 # The parameters of the reference's golden vectors (gpu-pir/params.cuh:65-71).
 FIXTURE_PARAMS = SpiralParams(n=1, pt_bits=8, t_exp_left=8, t_exp_right=8, t_gsw=8, t_conv=4,

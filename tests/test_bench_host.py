@@ -1,0 +1,35 @@
+"""Host logic of bench.py on CPU: clock summaries over the timed windows,
+the peak and traffic figures it reads from committed files, and the
+workload's image size against the library's layout rule."""
+import bench
+from spiralpir import params as P
+
+
+def test_clock_summary_counts_only_timed_windows():
+    c = bench.ClockSampler(0)
+    # (time, sm MHz, max MHz, W, reasons): sw_power_cap at t=1, hw_slowdown at t=9
+    c.samples = [(1.0, 2000.0, 2070.0, 500.0, 0x4), (2.0, 2070.0, 2070.0, 800.0, 0x0),
+                 (3.0, 2070.0, 2070.0, 700.0, 0x1), (9.0, 900.0, 2070.0, 100.0, 0x8)]
+    s = c.summary([(0.5, 3.5)])
+    assert s["samples"] == 3 and s["sm_mhz"] == 2070.0 and s["sm_min_mhz"] == 2000.0
+    assert s["power_w_max"] == 800.0 and s["reasons"] == ["sw_power_cap"]   # gpu_idle is not a reason
+    assert s["timed_s"] == 3.0
+    s = c.summary([(8.0, 10.0)])
+    assert s["reasons"] == ["hw_slowdown"] and s["sm_mhz"] == 900.0
+    assert c.summary([(20.0, 21.0)]) is None
+
+
+def test_peaks_and_traffic_from_committed_files():
+    peak, kind = bench.measured_peaks()
+    assert kind in ("measured", "fallback") and peak > 1000
+    tpeak, _ = bench.measured_peaks("bf16_tflops")
+    assert tpeak > 100
+    traffic = bench.ncu_traffic()
+    assert traffic is None or 7.0e9 < traffic < 8.0e9
+
+
+def test_workload_image_size_matches_layout():
+    sh = P.SHAPE_1GIB
+    assert P.PARAMS.db_device_bytes(sh.nu1, sh.nu2) == bench.WORKLOAD["db_device_bytes"] == 7 << 30
+    # packed 28-bit residues: 7 bytes per plaintext coefficient
+    assert P.PARAMS.db_device_bytes(sh.nu1, sh.nu2) == sh.num_records * P.PARAMS.T * P.D * 7
