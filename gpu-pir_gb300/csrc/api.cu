@@ -1790,6 +1790,8 @@ int ctx_view(sp_ctx *c, CtxView *out) {
     out->tw = c->d_tw;
     out->params = c->sp;
     out->mu = &c->mu;
+    out->device = c->device;
+    out->checked = c->checked;
     return SP_OK;
 }
 

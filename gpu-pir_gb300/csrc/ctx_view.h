@@ -13,6 +13,8 @@ struct CtxView {
     const TwiddleSet *tw;
     StageParams params;
     std::mutex *mu;
+    int device;      // the GPU the context (its stream, memory) lives on
+    bool checked;    // checked mode (guard regions verified after calls)
 };
 
 // Fills `out` for a live context; returns SP_OK or an error code.

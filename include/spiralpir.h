@@ -240,17 +240,21 @@ int sp_db_mul_batch(sp_ctx *ctx, int32_t db_id, int32_t nq, const uint64_t *sel,
  *   -> out uint64[T][2][D] raw.  (G - C is derived, not passed.) */
 int sp_fold(sp_ctx *ctx, const uint64_t *cts, const uint64_t *gsw, int32_t T, int32_t nu2, uint64_t *out);
 /* Fold without allocating device memory: same inputs, output and result as
- * sp_fold, for callers that may not call cudaMalloc at that point (inside a
- * stream capture, under an external allocator, or after a start-up-only
- * allocation phase).  No counterpart in the reference.  Device storage is a
- * fixed 8 MiB + 4 KiB array the library declares per GPU, held until the
- * process exits; inputs needing more than that (T * 2^nu2 * 32 KiB of
- * ciphertexts plus 24 * nu2 * t_gsw KiB of GSW ciphertexts) are rejected with
- * SP_ERR_INVALID.  The first call on a device resolves the array's device
- * address (cudaGetSymbolAddress); make that first call before any stream
- * capture.  All calls share the one array: calls are serialised by a
- * process-wide lock and each waits for its own GPU work, since two calls
- * overlapping on the GPU would race on it. */
+ * sp_fold, for callers that may not call cudaMalloc at that point (a process
+ * whose device memory another allocator already holds, or a service that
+ * allocates only at start-up).  No counterpart in the reference.  Device
+ * storage is a fixed 8 MiB + 4 KiB array the library declares per GPU, held
+ * until the process exits; inputs needing more than 8 MiB (T * 2^nu2 * 32 KiB
+ * of ciphertexts plus nu2 * t_gsw * 192 KiB for the GSW ciphertexts, as
+ * uploaded and in Montgomery form) are rejected with SP_ERR_INVALID.  The
+ * call runs on the context's GPU whatever device the calling thread has
+ * current (restored on return).  The first call for a GPU resolves the
+ * array's device address there (cudaGetSymbolAddress); make that first call
+ * before any stream capture.  All calls share the one array: calls are
+ * serialised by a process-wide lock and each waits for its own GPU work,
+ * since two calls overlapping on the GPU would race on it.  In checked mode a
+ * guard region after the call's data in the array is verified after the
+ * fold. */
 int sp_fold_noalloc(sp_ctx *ctx, const uint64_t *cts, const uint64_t *gsw, int32_t T, int32_t nu2, uint64_t *out);
 /* Pack n*n raw ciphertexts uint64[n*n][2][D] with the client's packing
  * keys, modulus-switch and serialise into `response`. */
