@@ -18,8 +18,12 @@ Printed as one JSON line (rank 0):
           D2H inside the timed region), host wall clock
   roofline  first-dimension multiply: algorithmic bytes / CUDA-event launch
           time against the measured HBM copy bandwidth
-  cpu_baseline  the CPU oracle on this host's cores, on a bounded sample of
-          the same workload, extrapolated to queries/s
+  cpu_baseline  the CPU oracle (the reference's answer path restated in C,
+          OpenMP on this host's cores) answering one full 1 GiB query, timed;
+          its response is compared byte for byte with the GPU's
+  parity  config2_bytes_equal (GPU response == CPU oracle response) and
+          batched_bytes_equal (every response of the B = 32 and B = 64
+          batches == the same query answered alone)
 With --gpus N > 1 (torchrun), every rank answers its own queries against its
 own replica of the database ("replicas only": the path does not shard here).
 """
@@ -202,21 +206,22 @@ def measured_peaks(key: str = "hbm_gbs"):
     return (6800.0 if key == "hbm_gbs" else 1900.0), "fallback"
 
 
-def ncu_traffic():
-    """DRAM bytes per multiply launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "db_mul_1gib.md")
+def measured_traffic(algo_bytes: float):
+    """DRAM bytes of one k_db_mul launch at the benchmark's size, scaled from
+    the ncu capture of a smaller case (profiles/db_mul_traffic.json: its
+    DRAM bytes over its algorithmic bytes; the multiply's traffic grows in
+    proportion to the image it streams), or None without a capture."""
+    path = os.path.join(ROOT, "profiles", "db_mul_traffic.json")
     if not os.path.exists(path):
         return None
-    for line in open(path):
-        if line.strip().startswith("dram_bytes_per_launch:"):
-            try:
-                return float(line.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
-    return None
+    with open(path) as f:
+        d = json.load(f)
+    return float(d["traffic_over_algorithmic"]) * algo_bytes
 
 
-def make_workload(seed: int = 0):
+def make_workload(seed: int = 0, n_queries: int = 64):
+    """The 1 GiB database, a seeded client with its public keys, and
+    `n_queries` queries for distinct seeded records."""
     from spiralpir import client as C
     from spiralpir import params as P
 
@@ -225,66 +230,77 @@ def make_workload(seed: int = 0):
     keys = cl.public_keys(sh.nu1, sh.nu2)
     recs = C.random_records(sh, p, seed=seed + 2)
     rng = np.random.default_rng(seed + 3)
-    idx = [int(x) for x in rng.integers(0, sh.num_records, size=8)]
+    idx = [int(x) for x in rng.choice(sh.num_records, size=n_queries, replace=False)]
     queries = [cl.query(sh, i) for i in idx]
     return p, sh, cl, keys, recs, idx, queries
 
 
-def cpu_baseline(threads: int | None = None) -> dict:
-    """Time the CPU oracle on a bounded sample of the 1 GiB answer and
-    extrapolate to one full query: full expansion and conversion, the
-    first-dimension multiply over 8 of 256 columns (x32), the fold of
-    2^3-column instances (x255/7) and the packing."""
-    import oracle as O
+class CpuOracle:
+    """The CPU oracle (the C restatement of the reference's answer path, with
+    OpenMP over the host's cores) holding the 1 GiB database encoded into
+    CRT-NTT form on the host (8 GiB of u32 planes; encoding is set-up, not
+    timed)."""
 
-    rng = np.random.default_rng(9)
+    def __init__(self, p, sh, recs, keys, threads: int | None = None):
+        import oracle as O
 
-    def residues(shape):
-        out = np.empty(tuple(shape) + (2, 2048), dtype=np.uint32)
-        out[..., 0, :] = rng.integers(0, O.Q1, size=tuple(shape) + (2048,), dtype=np.uint32)
-        out[..., 1, :] = rng.integers(0, O.Q2, size=tuple(shape) + (2048,), dtype=np.uint32)
-        return out
+        self.O, self.p, self.sh, self.keys = O, p, sh, keys
+        if threads:
+            O.set_threads(threads)
+        self.cores = O.num_threads()
+        t0 = time.perf_counter()
+        self.db = O.db_encode(recs, p.n, sh.nu1, sh.nu2, p.pt_bits)
+        self.encode_s = time.perf_counter() - t0
 
-    if threads:
-        O.set_threads(threads)
-    nth = O.num_threads()
-    n, nu1, nu2, tl, tg, tc = 2, 9, 8, 8, 7, 4
-    g = O.expansion_g(nu1, nu2, tg)
-    stop = O.expansion_stop(nu2, tg)
-    q = residues((2,))
-    left = residues((g, 2, tl))
-    right = residues((stop + 1, 2, tl))
-    t0 = time.perf_counter()
-    v = O.expand(q, left, tl, right, tl, nu1, nu2, tg)
-    t_exp = time.perf_counter() - t0
-    regev = np.ascontiguousarray(v[1:2 * nu2 * tg:2])
-    conv = residues((2, 2 * tc))
-    t0 = time.perf_counter()
-    gsw = O.regev_to_gsw(regev, conv, nu2, tg, tc)
-    neg = O.gsw_neg(gsw, tg)
-    t_conv = time.perf_counter() - t0
-    sample_cols = 3
-    db = residues((4, 1 << sample_cols, 1 << nu1))
-    sel = np.ascontiguousarray(v[0:2 << nu1:2])
-    t0 = time.perf_counter()
-    acc = O.db_mul(db, sel, 4, nu1, sample_cols)
-    raw = O.from_ntt(acc)
-    t_mul = (time.perf_counter() - t0) * (1 << (nu2 - sample_cols))
-    t0 = time.perf_counter()
-    folded = O.fold(raw, gsw[-sample_cols:], neg[-sample_cols:], sample_cols, tg)
-    t_fold = (time.perf_counter() - t0) * ((1 << nu2) - 1) / ((1 << sample_cols) - 1)
-    keys = residues((n, n + 1, tc))
-    t0 = time.perf_counter()
-    packed = O.pack(folded, keys, n, tc)
-    O.encode_response(packed, n, 8, 22)
-    t_pack = time.perf_counter() - t0
-    per_query = t_exp + t_conv + t_mul + t_fold + t_pack
-    return {"value": 1.0 / per_query, "unit": UNIT, "cores": nth, "kind": "port",
-            "seconds_per_query": per_query,
-            "stages_s": {"expand": t_exp, "convert": t_conv, "db_mul": t_mul, "fold": t_fold, "pack": t_pack},
-            "sample": "C oracle (OpenMP) on one 1 GiB-shape query: full expansion (g=10) and conversion; "
-                      "first-dimension multiply over 8 of 256 columns scaled x32; fold of 8-column "
-                      "instances scaled by 255/7 folds; packing"}
+    def answer(self, q) -> tuple[np.ndarray, float]:
+        """Full answer of one query (expansion, conversion, the multiply over
+        all 2^nu2 columns, all 2^nu2 - 1 folds per instance, packing);
+        returns the response bytes and the seconds it took."""
+        p, sh, k = self.p, self.sh, self.keys
+        t0 = time.perf_counter()
+        resp = self.O.answer(self.db, q, k.exp_left, k.exp_right, k.conv, k.pack, n=p.n, nu1=sh.nu1, nu2=sh.nu2,
+                             pt_bits=p.pt_bits, q2_bits=p.q2_bits, t_left=p.t_exp_left, t_right=p.t_exp_right,
+                             t_gsw=p.t_gsw, t_conv=p.t_conv)
+        return resp, time.perf_counter() - t0
+
+    def db_mul_s(self, nu1: int, nu2: int, reps: int = 1) -> float:
+        """Seconds per query of the first-dimension multiply alone (the
+        reference's CPU loop, gpu-pir/db_mul_test.cu:240-282: 128-bit
+        accumulation then one reduction, restated in C) at shape (nu1, nu2)
+        on seeded residues."""
+        O, T = self.O, self.p.T
+        rng = np.random.default_rng(nu1 * 100 + nu2)
+
+        def residues(shape):
+            out = np.empty(tuple(shape) + (2, 2048), dtype=np.uint32)
+            out[..., 0, :] = rng.integers(0, O.Q1, size=tuple(shape) + (2048,), dtype=np.uint32)
+            out[..., 1, :] = rng.integers(0, O.Q2, size=tuple(shape) + (2048,), dtype=np.uint32)
+            return out
+
+        db = self.db if (nu1, nu2) == (self.sh.nu1, self.sh.nu2) else residues((T, 1 << nu2, 1 << nu1))
+        sel = residues((1 << nu1, 2))
+        O.db_mul(db, sel, T, nu1, nu2)
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            O.db_mul(db, sel, T, nu1, nu2)
+        return (time.perf_counter() - t0) / reps
+
+
+def cpu_baseline(orc: CpuOracle, q, gpu_resp: np.ndarray) -> dict:
+    """One full 1 GiB query answered by the CPU oracle on this host's cores,
+    timed; its response bytes are compared with the GPU's response to the
+    same query.  Also times the first-dimension multiply alone (the
+    reference's CPU loop restated) at the 8 MiB, 64 MiB and 1 GiB shapes."""
+    resp, secs = orc.answer(q)
+    mul = {name: orc.db_mul_s(nu1, nu2, reps) * 1e3
+           for name, nu1, nu2, reps in (("8MiB", 7, 3, 20), ("64MiB", 8, 5, 4), ("1GiB", 9, 8, 1))}
+    return {"value": 1.0 / secs, "unit": UNIT, "cores": orc.cores, "kind": "port",
+            "seconds_per_query": secs, "db_encode_s": orc.encode_s,
+            "bytes_equal_to_gpu": bool(np.array_equal(resp, gpu_resp)),
+            "db_mul_ms_per_query": mul,
+            "sample": "one full 1 GiB query (all 256 columns of the multiply, all 255 folds per "
+                      "instance) by the C oracle with OpenMP; the database encoded on the host "
+                      "beforehand (not timed)"}
 
 
 def max_over_ranks(values, world: int) -> list:
@@ -300,23 +316,35 @@ def max_over_ranks(values, world: int) -> list:
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the CPU oracle (the reference's answer path restated
+    in C, OpenMP over all host cores) answering full 1 GiB queries, one query
+    per step, on rank 0 only."""
     if rank != 0:
         return
+    p, sh, cl, keys, recs, idx, queries = make_workload(seed=0, n_queries=8)
+    orc = CpuOracle(p, sh, recs, keys)
+    resp, _ = orc.answer(queries[0])
+    decoded = bool(np.array_equal(cl.decode(resp), recs[idx[0]]))
+    for i in range(1, args.warmup):
+        orc.answer(queries[i % len(queries)])
     ts = []
-    for i in range(args.warmup + args.steps):
-        r = cpu_baseline()
-        if i >= args.warmup:
-            ts.append(r["seconds_per_query"])
+    t_all = time.perf_counter()
+    for i in range(args.steps):
+        ts.append(orc.answer(queries[i % len(queries)])[1])
+    wall = time.perf_counter() - t_all
     per = sum(ts) / len(ts)
-    cb = cpu_baseline.__doc__
     line = {"metric": METRIC, "value": 1.0 / per, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u32 (exact modular)", "data": "synthetic", "config": WORKLOAD,
             "impl": "reference",
-            "cpu_baseline": {"value": 1.0 / per, "unit": UNIT, "cores": r["cores"], "kind": "port",
-                             "sample": r["sample"]},
+            "cpu_baseline": {"value": 1.0 / per, "unit": UNIT, "cores": orc.cores, "kind": "port",
+                             "sample": "one full 1 GiB query per step (all 256 columns, all 255 folds per "
+                                       "instance); the database encoded on the host before the first step"},
             "e2e": {"value": 1.0 / per, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": " ".join(cb.split()) if cb else ""}
+            "timed_wall_s": wall, "db_encode_s": orc.encode_s, "decoded_ok": decoded,
+            "note": "The reference ships no runnable CPU answer path (its CUDA does not compile as shipped and "
+                    "its Python model is thread-faithful and about 1.4 s per fold), so this arm runs the C "
+                    "oracle that restates the reference's algorithms (kind: port)."}
     print(json.dumps(line), flush=True)
 
 
@@ -331,8 +359,8 @@ def run_gpu(args, rank, world, local):
     gpu.load_db(1, recs, sh.nu1, sh.nu2)
     load_s = time.perf_counter() - t0
     # correctness of the measured configuration
-    resp = gpu.answer(1, 1, queries[0])
-    ok = bool(np.array_equal(cl.decode(resp), recs[idx[0]]))
+    resp0 = gpu.answer(1, 1, queries[0])
+    ok = bool(np.array_equal(cl.decode(resp0), recs[idx[0]]))
     if not ok:
         raise SystemExit("decoded record differs from the database record")
     barrier = None
@@ -379,10 +407,14 @@ def run_gpu(args, rank, world, local):
     clk = clocks.summary(clocks.windows)
     if barrier:
         barrier()
-    # batched answering (B queries per pipeline run), same database
+    # batched answering (B queries per pipeline run), same database; every
+    # batched response is compared byte for byte with the same query
+    # answered alone and decoded
     batched = None
+    batch_equal, batch_decoded = True, True
     if args.batched > 1:
         sizes = [args.batched, 2 * args.batched]
+        alone = [gpu.answer(1, 1, queries[s % len(queries)]) for s in range(max(sizes))]
         gpu2 = SpiralGPU(p, max_batch=max(sizes))
         gpu2.set_client_keys(1, keys)
         gpu2.load_db(1, recs, sh.nu1, sh.nu2)
@@ -396,9 +428,15 @@ def run_gpu(args, rank, world, local):
             gpu2.stats_reset()
             gpu2.run_staged(B)
             bsplit = gpu2.stats()
-            rb = gpu2.fetch_response(3 % B)
-            assert np.array_equal(cl.decode(rb), recs[idx[3 % B % len(idx)]])
+            eq = dec = 0
+            for s in range(B):
+                rb = gpu2.fetch_response(s)
+                eq += bool(np.array_equal(rb, alone[s]))
+                dec += bool(np.array_equal(cl.decode(rb), recs[idx[s % len(idx)]]))
+            batch_equal = batch_equal and eq == B
+            batch_decoded = batch_decoded and dec == B
             entry = {"B": B, "queries_per_s": B / (bms / 1e3), "ms_per_batch": bms,
+                     "distinct_queries": min(B, len(queries)), "bytes_equal_single": eq, "decoded_ok": dec,
                      "speedup_vs_single": (B / bms) / (batch / ms),
                      "db_mul_variant": 1 + int(np.argmax(bsplit["db_mul_by_variant"])),
                      "stages_ms": {k[3:]: bsplit[k] for k in
@@ -427,7 +465,7 @@ def run_gpu(args, rank, world, local):
     algo_bytes = sh.num_records * p.T * 2048 * 7 + (sh.rows * 2048 * 16 + p.T * sh.cols * 4 * 2048 * 4) * batch
     peak, peak_kind = measured_peaks()
     achieved = algo_bytes / (mul_ms / 1e3) / 1e9
-    traffic = ncu_traffic()
+    traffic = measured_traffic(algo_bytes)
     lat_ms = sorted(x * 1e3 for x in lat)
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / batch, "higher_is_better": True,
@@ -444,9 +482,14 @@ def run_gpu(args, rank, world, local):
                           ("ms_expand", "ms_convert", "ms_db_mul", "ms_fold", "ms_pack", "ms_total")},
             "gpu_launches": int(st["launches"]), "launches_per_answer": launches_per_answer,
             "batched": batched, "clocks": clk, "db_load_s": load_s, "decoded_ok": ok}
-    if rank == 0:
-        line["cpu_baseline"] = cpu_baseline()
     gpu.close()
+    if rank == 0:
+        orc = CpuOracle(p, sh, recs, keys)
+        line["cpu_baseline"] = cpu_baseline(orc, queries[0], resp0)
+        del orc
+        line["parity"] = {"config2_bytes_equal": line["cpu_baseline"]["bytes_equal_to_gpu"],
+                          "batched_bytes_equal": batch_equal if batched else None,
+                          "batched_decoded_ok": batch_decoded if batched else None}
     if world > 1:
         # the slowest rank sets the whole job's time
         ms_max, e2e_max = max_over_ranks([ms, e2e_s], world)
@@ -462,7 +505,7 @@ def run_gpu(args, rank, world, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--batch", type=int, default=1, help="queries per step (1 = plain single-query path)")

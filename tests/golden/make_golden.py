@@ -1,6 +1,6 @@
 """Regenerate tests/golden/golden.json.
 
-    python tests/golden/make_golden.py [--ref /root/reference/gpu-pir]
+    python tests/golden/make_golden.py [--ref <reference checkout>/gpu-pir]
 
 1. Pins the CPU oracle: when the reference tree is present, the oracle must
    reproduce the reference's golden vectors (gpu-pir/test_data/*.dat: NTT,
@@ -78,9 +78,14 @@ def pin_against_reference_python(cpu_dir: str) -> None:
     print("oracle reproduces the reference cpu_version on seeded inputs")
 
 
+def _reference_root() -> str:
+    """$SPIRAL_REF_ROOT, else a `reference` directory beside the repository."""
+    return os.environ.get("SPIRAL_REF_ROOT") or os.path.join(os.path.dirname(ROOT), "reference")
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference/gpu-pir")
+    ap.add_argument("--ref", default=os.path.join(_reference_root(), "gpu-pir"))
     args = ap.parse_args()
     if os.path.isdir(os.path.join(args.ref, "test_data")):
         pin_against_reference_vectors(os.path.join(args.ref, "test_data"))

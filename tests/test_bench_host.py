@@ -24,8 +24,9 @@ def test_peaks_and_traffic_from_committed_files():
     assert kind in ("measured", "fallback") and peak > 1000
     tpeak, _ = bench.measured_peaks("bf16_tflops")
     assert tpeak > 100
-    traffic = bench.ncu_traffic()
-    assert traffic is None or 7.0e9 < traffic < 8.0e9
+    algo = 7_566_524_416
+    traffic = bench.measured_traffic(algo)
+    assert traffic is None or 0.95 * algo < traffic < 1.2 * algo
 
 
 def test_workload_image_size_matches_layout():
@@ -33,3 +34,18 @@ def test_workload_image_size_matches_layout():
     assert P.PARAMS.db_device_bytes(sh.nu1, sh.nu2) == bench.WORKLOAD["db_device_bytes"] == 7 << 30
     # packed 28-bit residues: 7 bytes per plaintext coefficient
     assert P.PARAMS.db_device_bytes(sh.nu1, sh.nu2) == sh.num_records * P.PARAMS.T * P.D * 7
+
+
+def test_cpu_oracle_small_shape_matches_itself_and_decodes():
+    """The CPU leg on a small shape: a full answer, timed, decodes to the
+    record; the multiply timer runs at a shape other than the database's."""
+    from spiralpir import client as C
+
+    p, sh = P.PARAMS, P.DbShape(7, 3)
+    cl = C.Client(p, seed=5)
+    keys = cl.public_keys(sh.nu1, sh.nu2)
+    recs = C.random_records(sh, p, seed=6)
+    orc = bench.CpuOracle(p, sh, recs, keys)
+    resp, secs = orc.answer(cl.query(sh, 9))
+    assert secs > 0 and (cl.decode(resp) == recs[9]).all()
+    assert orc.db_mul_s(6, 2) > 0
