@@ -14,7 +14,7 @@ namespace sp {
 namespace {
 
 constexpr int THREADS = 256;
-// shared memory: 4 twiddle tables + per group 2 transpose buffers
+// shared memory: 2 twiddle tables + per group 2 transpose buffers
 constexpr int SMEM_WORDS = TW_WORDS + 2 * 2 * D;
 constexpr int SMEM_BYTES = SMEM_WORDS * 4;
 
@@ -37,7 +37,7 @@ cudaError_t launch_ex(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t sm
 }
 
 struct Ctx {
-    const uint32_t *tw;   // 4 tables (TW_WORDS words)
+    const uint32_t *tw;   // 2 tables (TW_WORDS words)
     uint32_t *buf;   // this group's two transpose buffers
     uint32_t *bufs;  // both groups' buffers (exchange area, 4*D words)
     Prime c;
@@ -59,7 +59,8 @@ __device__ __forceinline__ Ctx setup(uint32_t *smem, const TwiddleSet *tws) {
 }
 
 __device__ __forceinline__ const uint2 *tw_fwd(const Ctx &x) { return tw_of(x.tw, x.g); }
-__device__ __forceinline__ const uint2 *tw_inv(const Ctx &x) { return tw_of(x.tw, 2 + x.g); }
+// the inverse transforms read the forward table too (common.cuh)
+__device__ __forceinline__ const uint2 *tw_inv(const Ctx &x) { return tw_of(x.tw, x.g); }
 
 // Both groups hold unscaled INTT outputs (layout A, < 2p) of the same
 // polynomial mod their prime; returns the raw coefficients of this thread's
@@ -191,7 +192,7 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_expand_round(const QDesc *
     const Prime c = prime_of(g);
     uint32_t *bufs = smem + TW_WORDS;
     uint32_t *buf = bufs + gi * 2 * D;
-    const uint2 *twf = tw_of(smem, g), *twi = tw_of(smem, 2 + g);
+    const uint2 *twf = tw_of(smem, g), *twi = twf;
     __syncthreads();
     const int half = 1 << r;
     const bool upper = i >= half;
@@ -322,7 +323,7 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_expand_round(const QDesc *
 
 cudaError_t launch_expand_round(const QDesc *qd, int nq, int r, int max_out, const StageParams &sp,
                                 const TwiddleSet *tw, const uint32_t *neg1, const SplitScratch *scr,
-                                cudaStream_t st) {
+                                cudaStream_t st, int split_shift) {
     const uint64_t total = (uint64_t)max_out * nq;
     const int sms = sm_count();
     if (total < 2ull * sms) {
@@ -332,7 +333,8 @@ cudaError_t launch_expand_round(const QDesc *qd, int nq, int r, int max_out, con
         int split = 1;
         if (scr && scr->part) {
             const int digits = std::max(sp.t_left, sp.t_right);
-            split = (int)std::min<uint64_t>(std::max<uint64_t>(1, sms / total), (uint64_t)(digits + 1) / 2);
+            split = shifted_split((int)std::min<uint64_t>(std::max<uint64_t>(1, sms / total), (uint64_t)(digits + 1) / 2),
+                                  split_shift, (digits + 1) / 2);
             while (split > 1 && (total * split > (uint64_t)scr->slots || total > (uint64_t)scr->counter_slots)) split--;
         }
         const int smem = (TW_WORDS + 4 * 2 * D) * 4 + D * 8;
@@ -533,7 +535,7 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_fold_level(const QDesc *__
     const Prime c = prime_of(g);
     uint32_t *bufs = smem + TW_WORDS;           // [group][2][D]
     uint32_t *buf = bufs + gi * 2 * D;
-    const uint2 *twf = tw_of(smem, g), *twi = tw_of(smem, 2 + g);
+    const uint2 *twf = tw_of(smem, g), *twi = twf;
     __syncthreads();
     const int cols = 1 << Q.nu2;
     uint64_t *base = Q.raw + (size_t)inst * cols * 2 * D;
@@ -550,30 +552,31 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_fold_level(const QDesc *__
     for (int pr = s * GP + sub; pr < 2 * tg; pr += GP * split) {
         const int row = pr / tg, k = pr % tg;
         const int sh = bits * k;
-        // digit k of both inputs from 32-bit words: a funnel shift of the two
-        // halves below bit 32, the high half alone above
+        // digit k of both inputs from 32-bit words: one word when the digit
+        // lies in one half of the 64-bit value (fewer live registers), a
+        // funnel shift of both halves when it straddles bit 32
         uint32_t d[VPT];
         const uint32_t m32 = (uint32_t)mask;
-        if (sh < 32) {
-            const uint2 *w1 = reinterpret_cast<const uint2 *>(v1 + row * D);
-            const uint2 *w0 = reinterpret_cast<const uint2 *>(v0 + row * D);
+        const uint32_t *w1 = reinterpret_cast<const uint32_t *>(v1 + row * D);
+        const uint32_t *w0 = reinterpret_cast<const uint32_t *>(v0 + row * D);
+        if (sh + bits <= 32 || sh >= 32) {
+            const int hw = sh >= 32, s2 = sh - 32 * hw;
 #pragma unroll
             for (int j = 0; j < VPT; j++) {
                 const int e = t + GROUP * j;
-                const uint2 x1 = __ldg(w1 + e), x0 = w0[e];
-                const uint32_t a = __funnelshift_r(x1.x, x1.y, sh) & m32;
-                const uint32_t b = __funnelshift_r(x0.x, x0.y, sh) & m32;
+                const uint32_t a = (__ldg(w1 + 2 * e + hw) >> s2) & m32;
+                const uint32_t b = (w0[2 * e + hw] >> s2) & m32;
                 d[j] = a >= b ? a - b : a + c.p - b;
             }
         } else {
-            const uint32_t *h1 = reinterpret_cast<const uint32_t *>(v1 + row * D) + 1;
-            const uint32_t *h0 = reinterpret_cast<const uint32_t *>(v0 + row * D) + 1;
-            const int s2 = sh - 32;
+            const uint2 *u1 = reinterpret_cast<const uint2 *>(w1);
+            const uint2 *u0 = reinterpret_cast<const uint2 *>(w0);
 #pragma unroll
             for (int j = 0; j < VPT; j++) {
                 const int e = t + GROUP * j;
-                const uint32_t a = (__ldg(h1 + 2 * e) >> s2) & m32;
-                const uint32_t b = (h0[2 * e] >> s2) & m32;
+                const uint2 x1 = __ldg(u1 + e), x0 = u0[e];
+                const uint32_t a = __funnelshift_r(x1.x, x1.y, sh) & m32;
+                const uint32_t b = __funnelshift_r(x0.x, x0.y, sh) & m32;
                 d[j] = a >= b ? a - b : a + c.p - b;
             }
         }
@@ -649,7 +652,7 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_fold_level(const QDesc *__
 }
 
 cudaError_t launch_fold_level(const QDesc *qd, int nq, int level, int max_items, const StageParams &sp,
-                              const TwiddleSet *tw, const SplitScratch *scr, cudaStream_t st) {
+                              const TwiddleSet *tw, const SplitScratch *scr, cudaStream_t st, int split_shift) {
     const uint64_t total = (uint64_t)max_items * nq;
     const int sms = sm_count();
     if (total <= (uint64_t)sms) {
@@ -661,7 +664,8 @@ cudaError_t launch_fold_level(const QDesc *qd, int nq, int level, int max_items,
         // group
         int split = 1;
         if (scr && scr->part) {
-            split = (int)std::min<uint64_t>(std::max<uint64_t>(1, sms / total), (uint64_t)sp.t_gsw);
+            split = shifted_split((int)std::min<uint64_t>(std::max<uint64_t>(1, sms / total), (uint64_t)sp.t_gsw),
+                                  split_shift, sp.t_gsw);
             while (split > 1 && (total * split > (uint64_t)scr->slots || total > (uint64_t)scr->counter_slots)) split--;
         }
         const int smem = (TW_WORDS + 4 * 2 * D) * 4;
@@ -804,7 +808,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_pack(const QDesc *__restrict__ q
 }
 
 cudaError_t launch_pack(const QDesc *qd, int nq, const StageParams &sp, const TwiddleSet *tw,
-                        const SplitScratch *scr, cudaStream_t st) {
+                        const SplitScratch *scr, cudaStream_t st, int split_shift) {
     cudaError_t e = cudaFuncSetAttribute(k_pack, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     if (e != cudaSuccess) return e;
     // spread each column's n*(t_conv+1) transforms over CTAs while the launch
@@ -813,7 +817,8 @@ cudaError_t launch_pack(const QDesc *qd, int nq, const StageParams &sp, const Tw
     const int units = sp.n * (sp.t_conv + 1);
     int split = 1;
     if (scr && scr->part) {
-        split = (int)std::min<uint64_t>(std::max<uint64_t>(1, sm_count() / cols), (uint64_t)units);
+        split = shifted_split((int)std::min<uint64_t>(std::max<uint64_t>(1, sm_count() / cols), (uint64_t)units),
+                              split_shift, units);
         while (split > 1 && (cols * split * (sp.n + 1) * 2 > (uint64_t)scr->slots * 4 || cols > (uint64_t)scr->counter_slots))
             split--;
     }

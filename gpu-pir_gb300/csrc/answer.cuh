@@ -19,6 +19,19 @@ struct SplitScratch {
     uint32_t *counters = nullptr;   // [counter_slots], zero between launches
     int slots = 0, counter_slots = 0;
 };
+// Split schedules of the narrow launches (few items: an expansion round, a
+// fold level or the pack spreads each item over `split` CTAs).  The rule
+// gives split = min(SMs / items, cap); a schedule shifts it: shift s >= 0
+// multiplies it by 2^s, s < 0 divides it by 2^-s, SPLIT_NONE runs one CTA per
+// item; the result stays in [1, cap].  Chosen per batch class by the
+// autotuner (api.cu); every schedule gives the same residues.
+constexpr int SPLIT_NONE = -16;
+inline int shifted_split(int rule, int shift, int cap) {
+    if (shift <= SPLIT_NONE) return 1;
+    const int s = shift >= 0 ? rule << shift : rule >> -shift;
+    return s < 1 ? 1 : (s > cap ? cap : s);
+}
+
 // u64 canonical residues [count][2][D] -> u32 (optionally Montgomery form)
 cudaError_t launch_narrow(const uint64_t *in, uint32_t *out, uint64_t planes, bool to_mont, cudaStream_t st);
 // u32 [count][2][D] (optionally from Montgomery form) -> u64 canonical
@@ -32,16 +45,16 @@ cudaError_t launch_sel_import(const uint64_t *in, uint32_t *sel, int rows, cudaS
 
 cudaError_t launch_expand_round(const QDesc *qd, int nq, int r, int max_out, const StageParams &sp,
                                 const TwiddleSet *tw, const uint32_t *neg1, const SplitScratch *scr,
-                                cudaStream_t st);
+                                cudaStream_t st, int split_shift = 0);
 cudaError_t launch_regev_to_gsw(const QDesc *qd, int nq, int max_items, const StageParams &sp,
                                 const TwiddleSet *tw, cudaStream_t st);
 // G - C for count GSW ciphertexts (canonical in and out)
 cudaError_t launch_gsw_neg(const uint32_t *gsw, uint32_t *neg, int count, int t, cudaStream_t st);
 // scr == nullptr: no split (every item in one CTA)
 cudaError_t launch_fold_level(const QDesc *qd, int nq, int level, int max_items, const StageParams &sp,
-                              const TwiddleSet *tw, const SplitScratch *scr, cudaStream_t st);
+                              const TwiddleSet *tw, const SplitScratch *scr, cudaStream_t st, int split_shift = 0);
 cudaError_t launch_pack(const QDesc *qd, int nq, const StageParams &sp, const TwiddleSet *tw,
-                        const SplitScratch *scr, cudaStream_t st);
+                        const SplitScratch *scr, cudaStream_t st, int split_shift = 0);
 cudaError_t launch_bitpack(const QDesc *qd, int nq, const StageParams &sp, uint64_t resp_bytes,
                            cudaStream_t st);
 

@@ -19,6 +19,7 @@
 #include "../../include/spiralpir.h"
 #include "answer.cuh"
 #include "ctx_view.h"
+#include "seeded.cuh"
 
 using namespace sp;
 
@@ -182,6 +183,12 @@ struct sp_ctx {
     std::map<std::pair<int, int>, int> mul_choice;
     std::map<int, float> mul_single_ms;
     int mul_force = 0;          // 0 = autotune, 1..3 = force a variant
+    // split schedule of the narrow launches (answer.cuh shifted_split) per
+    // batch class (ceil log2 nq, deepest expansion, deepest fold): tuned on
+    // first use unless forced; and the tuner's log
+    int split_force = SP_SPLIT_AUTO;
+    std::map<std::vector<int64_t>, int> plan_split;
+    std::deque<std::string> tune_log;
     bool use_graphs = true;     // replay the answer pipeline as CUDA graphs
     // serving (continuous batching)
     std::vector<Lane *> lanes;
@@ -652,6 +659,41 @@ cudaError_t enqueue_inputs(Lane &L, int nq, cudaStream_t st) {
     return e;
 }
 
+// Autotuner of the narrow launches' split schedule (answer.cuh
+// shifted_split).  The pipeline is idempotent from its staged inputs, so each
+// candidate schedule runs it once (on the batch at hand), timed between the
+// first and the last stage event; the fastest is kept for the batch class
+// `key` = (ceil(log2 nq), deepest expansion, deepest fold); ties favour the
+// rule, shift 0.  Every schedule gives identical residues.  The class and the
+// candidate times go to the tuning log (sp_tuning_report).
+template <typename Enqueue>
+int tune_split(sp_ctx *c, Lane &L, const std::vector<int64_t> &key, Enqueue &enqueue, int *shift) {
+    static const int cands[] = {0, -1, 1, SPLIT_NONE};
+    float best_ms = 0;
+    int best = 0;
+    std::string msg = "plan class nq<=" + std::to_string(1ll << key[0]) + " g=" + std::to_string(key[1]) +
+                      " nu2=" + std::to_string(key[2]) + ":";
+    for (int cand : cands) {
+        *shift = cand;
+        CU(enqueue(false));
+        CU(cudaEventSynchronize(L.ev[5]));
+        float ms = 0;
+        CU(cudaEventElapsedTime(&ms, L.ev[0], L.ev[5]));
+        msg += " shift " + (cand == SPLIT_NONE ? std::string("none") : std::to_string(cand)) + " " +
+               std::to_string(ms).substr(0, 6) + " ms;";
+        if (cand == 0 || ms < best_ms * 0.99f) {
+            best_ms = ms;
+            best = cand;
+        }
+    }
+    *shift = best;
+    c->plan_split[key] = best;
+    msg += " chosen " + (best == SPLIT_NONE ? std::string("none") : std::to_string(best));
+    c->tune_log.push_back(msg);
+    while (c->tune_log.size() > 64) c->tune_log.pop_front();
+    return SP_OK;
+}
+
 // Run the answer pipeline for queries in slots [0, nq) (descriptors in
 // L.h_qd).  Without `io` the queries and descriptors are already on the
 // device (sp_stage_query); with `io` the pipeline itself uploads them from the
@@ -711,12 +753,13 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
     }
     // stage events are recorded as external event nodes so that a replayed
     // graph records them too
+    int cur_shift = 0;
     auto enqueue = [&](bool capturing) -> cudaError_t {
         const unsigned ev_flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
         cudaError_t e = io ? enqueue_inputs(L, nq, st) : cudaSuccess;
         if (!e) e = cudaEventRecordWithFlags(L.ev[0], st, ev_flags);
         for (int r = 0; r < max_g && !e; r++) {
-            e = launch_expand_round(L.d_qd, nq, r, 2 << r, sp, c->d_tw, c->d_neg1, &L.split, st);
+            e = launch_expand_round(L.d_qd, nq, r, 2 << r, sp, c->d_tw, c->d_neg1, &L.split, st, cur_shift);
             if (!e && r == fork_round) {
                 // the conversion needs only the GSW-bit encodings: run it on
                 // the side stream, overlapping the remaining rounds and the
@@ -737,9 +780,9 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
         if (!e) e = launch_acc_to_raw(L.d_qd, nq, sp.T * (2 << max_nu2), sp, c->d_tw, st);
         if (!e) e = cudaStreamWaitEvent(st, L.join_ev, 0);   // the folds need the GSW ciphertexts
         for (int lvl = 0; lvl < max_nu2 && !e; lvl++)
-            e = launch_fold_level(L.d_qd, nq, lvl, sp.T << (max_nu2 - 1 - lvl), sp, c->d_tw, &L.split, st);
+            e = launch_fold_level(L.d_qd, nq, lvl, sp.T << (max_nu2 - 1 - lvl), sp, c->d_tw, &L.split, st, cur_shift);
         if (!e) e = cudaEventRecordWithFlags(L.ev[4], st, ev_flags);
-        if (!e) e = launch_pack(L.d_qd, nq, sp, c->d_tw, &L.split, st);
+        if (!e) e = launch_pack(L.d_qd, nq, sp, c->d_tw, &L.split, st, cur_shift);
         if (!e) e = launch_bitpack(L.d_qd, nq, sp, response_bytes(sp), st);
         if (!e) e = cudaEventRecordWithFlags(L.ev[5], st, ev_flags);
         if (io) {
@@ -750,6 +793,23 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
         }
         return e;
     };
+    // split schedule: forced, tuned earlier for this batch class, or tuned
+    // now.  The class is what shapes the narrow launches: the batch size
+    // class ceil(log2 nq) and the deepest expansion and fold (so serving,
+    // where almost every batch mixes databases differently, tunes once per
+    // class, not per batch)
+    if (c->split_force != SP_SPLIT_AUTO) {
+        cur_shift = c->split_force;
+    } else {
+        const std::vector<int64_t> cls = {ceil_log2((uint64_t)nq), max_g, max_nu2};
+        auto ps = c->plan_split.find(cls);
+        if (ps != c->plan_split.end()) {
+            cur_shift = ps->second;
+        } else {
+            TRY(tune_split(c, L, cls, enqueue, &cur_shift));
+        }
+    }
+    key.push_back(cur_shift);
     auto it = L.graphs.find(key);
     bool replay = c->use_graphs && it != L.graphs.end();
     if (c->use_graphs && !replay && L.graphs.size() < 256) {
@@ -1202,13 +1262,18 @@ static int evict_lru(sp_ctx *c, uint64_t need) {
     return SP_OK;
 }
 
-int sp_client_set_keys(sp_ctx *c, int32_t client_id, const uint64_t *exp_left, int32_t n_left,
-                       const uint64_t *exp_right, int32_t n_right, const uint64_t *conv, const uint64_t *pack) {
-    if (!c || !exp_left || !exp_right || !conv || !pack) return fail(SP_ERR_INVALID, "NULL argument");
+}  // extern "C"
+
+namespace {
+
+// Registers client keys: `fill` enqueues on c->st the copies of the key
+// words into `u` (u64 staging in the device key layout: left | right | conv |
+// pack); with `seed`, row 0 of every key matrix is then regenerated on the
+// device from it (csrc/seeded.cu) instead of being copied.
+template <typename Fill>
+int set_keys_impl(sp_ctx *c, int32_t client_id, int32_t n_left, int32_t n_right, Fill fill, const SeedKey *seed) {
     if (n_left < 1 || n_left > LOGD || n_right < 1 || n_right > LOGD)
         return fail(SP_ERR_INVALID, "expansion key counts must be in [1, 11]");
-    std::lock_guard<std::mutex> lk(c->mu);
-    TraceRange trace_("sp_client_set_keys");
     const StageParams &s = c->sp;
     const uint64_t P = 2ull * D;   // words per NTT poly
     const uint64_t wl = (uint64_t)n_left * 2 * s.t_left * P, wr = (uint64_t)n_right * 2 * s.t_right * P;
@@ -1233,15 +1298,16 @@ int sp_client_set_keys(sp_ctx *c, int32_t client_id, const uint64_t *exp_left, i
         return rc;
     }
     uint64_t *u = up.as<uint64_t>();
-    cudaError_t e = cudaSuccess;
-    const uint64_t *src[4] = {exp_left, exp_right, conv, pack};
-    const uint64_t cnt[4] = {wl, wr, wc, wp};
-    uint64_t off = 0;
-    for (int i = 0; i < 4 && e == cudaSuccess; i++) {
-        e = cudaMemcpyAsync(u + off, src[i], cnt[i] * 8, cudaMemcpyHostToDevice, c->st);
-        off += cnt[i];
-    }
+    // seeded: the row-0 planes are regenerated below; clear them so that the
+    // conversion reads defined words
+    cudaError_t e = seed ? cudaMemsetAsync(u, 0, words * 8, c->st) : cudaSuccess;
+    if (e == cudaSuccess) e = fill(u, wl, wr, wc);
     if (e == cudaSuccess) e = launch_narrow(u, cl.keys, words / D, true, c->st);
+    if (e == cudaSuccess && seed) {
+        SeedRowMap m{n_left, s.t_left, n_right, s.t_right, s.t_conv, s.n,
+                     (uint32_t)(n_left * s.t_left + n_right * s.t_right + 2 * s.t_conv + s.n * s.t_conv)};
+        e = launch_seed_rows(*seed, m, cl.keys, c->st);
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
     if (e != cudaSuccess) {
         release(c, cl.keys, cl.bytes);
@@ -1254,6 +1320,65 @@ int sp_client_set_keys(sp_ctx *c, int32_t client_id, const uint64_t *exp_left, i
     cl.stamp = ++c->clock;
     c->clients[client_id] = cl;
     return SP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sp_client_set_keys(sp_ctx *c, int32_t client_id, const uint64_t *exp_left, int32_t n_left,
+                       const uint64_t *exp_right, int32_t n_right, const uint64_t *conv, const uint64_t *pack) {
+    if (!c || !exp_left || !exp_right || !conv || !pack) return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_client_set_keys");
+    const StageParams &s = c->sp;
+    auto fill = [&](uint64_t *u, uint64_t wl, uint64_t wr, uint64_t wc) {
+        const uint64_t wp = (uint64_t)s.n * (s.n + 1) * s.t_conv * 2 * D;
+        const uint64_t *src[4] = {exp_left, exp_right, conv, pack};
+        const uint64_t cnt[4] = {wl, wr, wc, wp};
+        uint64_t off = 0;
+        cudaError_t e = cudaSuccess;
+        for (int i = 0; i < 4 && e == cudaSuccess; i++) {
+            e = cudaMemcpyAsync(u + off, src[i], cnt[i] * 8, cudaMemcpyHostToDevice, c->st);
+            off += cnt[i];
+        }
+        return e;
+    };
+    return set_keys_impl(c, client_id, n_left, n_right, fill, nullptr);
+}
+
+int sp_client_set_keys_seeded(sp_ctx *c, int32_t client_id, const uint8_t *seed, const uint64_t *left_rest,
+                              int32_t n_left, const uint64_t *right_rest, int32_t n_right, const uint64_t *conv_rest,
+                              const uint64_t *pack_rest) {
+    if (!c || !seed || !left_rest || !right_rest || !conv_rest || !pack_rest)
+        return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_client_set_keys_seeded");
+    const StageParams &s = c->sp;
+    SeedKey key;
+    for (int i = 0; i < 8; i++)
+        key.w[i] = (uint32_t)seed[4 * i] | (uint32_t)seed[4 * i + 1] << 8 | (uint32_t)seed[4 * i + 2] << 16 |
+                   (uint32_t)seed[4 * i + 3] << 24;
+    // each matrix's rows below row 0 go to their place in the full layout
+    auto fill = [&](uint64_t *u, uint64_t wl, uint64_t wr, uint64_t wc) {
+        const uint64_t P = 2ull * D;
+        cudaError_t e = cudaSuccess;
+        for (int r = 0; r < n_left && e == cudaSuccess; r++)
+            e = cudaMemcpyAsync(u + ((uint64_t)r * 2 + 1) * s.t_left * P, left_rest + (uint64_t)r * s.t_left * P,
+                                (uint64_t)s.t_left * P * 8, cudaMemcpyHostToDevice, c->st);
+        for (int r = 0; r < n_right && e == cudaSuccess; r++)
+            e = cudaMemcpyAsync(u + wl + ((uint64_t)r * 2 + 1) * s.t_right * P, right_rest + (uint64_t)r * s.t_right * P,
+                                (uint64_t)s.t_right * P * 8, cudaMemcpyHostToDevice, c->st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(u + wl + wr + 2ull * s.t_conv * P, conv_rest, 2ull * s.t_conv * P * 8,
+                                cudaMemcpyHostToDevice, c->st);
+        for (int r = 0; r < s.n && e == cudaSuccess; r++)
+            e = cudaMemcpyAsync(u + wl + wr + wc + ((uint64_t)r * (s.n + 1) + 1) * s.t_conv * P,
+                                pack_rest + (uint64_t)r * s.n * s.t_conv * P, (uint64_t)s.n * s.t_conv * P * 8,
+                                cudaMemcpyHostToDevice, c->st);
+        return e;
+    };
+    return set_keys_impl(c, client_id, n_left, n_right, fill, &key);
 }
 
 int sp_client_evict(sp_ctx *c, int32_t client_id) {
@@ -1429,6 +1554,29 @@ int sp_set_db_mul_variant(sp_ctx *c, int32_t variant) {
     std::lock_guard<std::mutex> lk(c->mu);
     TraceRange trace_("sp_set_db_mul_variant");
     c->mul_force = variant;
+    return SP_OK;
+}
+
+int sp_set_split_schedule(sp_ctx *c, int32_t shift) {
+    if (!c) return fail(SP_ERR_INVALID, "NULL context");
+    if (shift != SP_SPLIT_AUTO && shift != SP_SPLIT_NONE && (shift < -4 || shift > 4))
+        return fail(SP_ERR_INVALID, "split shift must be SP_SPLIT_AUTO, SP_SPLIT_NONE or in [-4, 4]");
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->split_force = shift;
+    return SP_OK;
+}
+
+int sp_tuning_report(sp_ctx *c, char *buf, uint64_t len) {
+    if (!c || !buf || !len) return fail(SP_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(c->mu);
+    std::string out;
+    for (const auto &kv : c->mul_choice)
+        out += "multiply db " + std::to_string(kv.first.first) + " batch class 2^" + std::to_string(kv.first.second) +
+               ": variant " + std::to_string(kv.second) + "\n";
+    for (const std::string &m : c->tune_log) out += m + "\n";
+    const size_t n = std::min<size_t>(out.size(), len - 1);
+    std::memcpy(buf, out.data(), n);
+    buf[n] = 0;
     return SP_OK;
 }
 

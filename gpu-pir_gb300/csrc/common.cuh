@@ -13,9 +13,13 @@
 //   layout C: thread t holds e = 16*t + j         stages h = 4, 2, 1
 // Raw-domain work (digits, inverse CRT) uses layout A (coalesced), NTT-domain
 // work (key products) uses layout C (16 consecutive slots per thread).
-// Butterflies are Harvey's lazy Montgomery butterflies (values < 4p forward,
-// < 2p inverse); the transposes use an XOR swizzle that is bank-conflict free
-// for all three layouts.
+// Butterflies are Harvey's lazy butterflies with Shoup products (values < 4p
+// forward, < 2p inverse); the transposes use an XOR swizzle that is
+// bank-conflict free for all three layouts.  Both directions read one
+// twiddle table per prime: the inverse twiddle of block i at the stage with
+// m blocks, psi^-brev11(m+i), equals -psi^brev11(2m-1-i) (psi^2048 = -1), so
+// the inverse transform reads the forward entry 2m-1-i and folds the sign
+// into its butterfly.
 #pragma once
 #include <stdint.h>
 #include <cuda_runtime.h>
@@ -142,17 +146,17 @@ __host__ __device__ __forceinline__ constexpr int swz(int e) {
 }
 
 // --------------------------------------------------------- twiddle tables
-// Per (prime, direction): 2048 pairs (w, floor(w * 2^32 / p)) with w
-// canonical, for Shoup multiplication.  Entry m+i holds psi^(+-brev11(m+i))
-// (block i of the stage with m blocks) for m < 256; the last three stages
-// (m = 256, 512, 1024; c = m/128 twiddles per thread) are restrided so that
-// entry m + k*128 + t holds twiddle m + c*t + k.
+// Per prime: 2048 pairs (w, floor(w * 2^32 / p)) with w canonical, for Shoup
+// multiplication.  Entry m+i holds psi^brev11(m+i) (block i of the stage
+// with m blocks) for m < 256; the last three stages (m = 256, 512, 1024;
+// c = m/128 twiddles per thread) are restrided so that entry m + k*128 + t
+// holds twiddle m + c*t + k.
 struct TwiddleSet {
-    uint2 t[4][D];   // [fwd q1, fwd q2, inv q1, inv q2]
+    uint2 t[2][D];   // [q1, q2]
 };
-constexpr int TW_WORDS = 8 * D;   // u32 words of a TwiddleSet in shared memory
+constexpr int TW_WORDS = 4 * D;   // u32 words of a TwiddleSet in shared memory
 
-// Table k (0, 1 forward; 2, 3 inverse) of a TwiddleSet copied to shared memory.
+// Table k (prime k) of a TwiddleSet copied to shared memory.
 __device__ __forceinline__ const uint2 *tw_of(const uint32_t *smem_tw, int k) {
     return reinterpret_cast<const uint2 *>(smem_tw) + k * D;
 }
@@ -171,9 +175,11 @@ __device__ __forceinline__ void ct_bfly(uint32_t &x, uint32_t &y, uint2 w, uint3
     y = xr - t + 2 * p;
 }
 
-__device__ __forceinline__ void gs_bfly(uint32_t &x, uint32_t &y, uint2 w, uint32_t p) {
+// Gentleman-Sande butterfly with the twiddle -w: x + y and (x - y)(-w) =
+// (y - x) w, both in [0, 2p) for inputs below 2p.
+__device__ __forceinline__ void gs_bfly_neg(uint32_t &x, uint32_t &y, uint2 w, uint32_t p) {
     uint32_t s = x + y;
-    uint32_t d = x - y + 2 * p;
+    uint32_t d = y - x + 2 * p;
     x = min(s, s - 2 * p);
     y = shoup_mul(d, w.x, w.y, p);
 }
@@ -242,16 +248,19 @@ __device__ __forceinline__ void ntt_fwd(uint32_t (&v)[VPT], const uint2 *__restr
 }
 
 // Inverse NTT of one plane (without the 2048^-1 scaling).  v: layout C in
-// (values < 2p), layout A out (values < 2p).
+// (values < 2p), layout A out (values < 2p).  tw: this prime's FORWARD
+// table: block i of the stage with m blocks uses -tw[2m-1-i] (in the
+// restrided stages block c*t + k is entry m + (c-1-k)*128 + (127-t)).
 __device__ __forceinline__ void ntt_inv(uint32_t (&v)[VPT], const uint2 *__restrict__ tw,
                                         uint32_t *buf, const Prime &c, int t, int bar_id) {
     const uint32_t p = c.p;
 #pragma unroll
     for (int L = 10; L >= 8; L--) {
-        const int dj = 4 >> (L - 8);
+        const int dj = 4 >> (L - 8), cs = (1 << L) / GROUP;
 #pragma unroll
         for (int j = 0; j < VPT; j++)
-            if ((j & dj) == 0) gs_bfly(v[j], v[j + dj], tw[(1 << L) + (j / (2 * dj)) * GROUP + t], p);
+            if ((j & dj) == 0)
+                gs_bfly_neg(v[j], v[j + dj], tw[(1 << L) + (cs - 1 - j / (2 * dj)) * GROUP + (GROUP - 1 - t)], p);
     }
     {
         uint32_t *b0 = buf;
@@ -271,7 +280,7 @@ __device__ __forceinline__ void ntt_inv(uint32_t (&v)[VPT], const uint2 *__restr
 #pragma unroll
             for (int j = 0; j < VPT; j++)
                 if ((j & dj) == 0)
-                    gs_bfly(v[j], v[j + dj], tw[(1 << L) + (bb << (L - 4)) + (j >> (8 - L))], p);
+                    gs_bfly_neg(v[j], v[j + dj], tw[(2 << L) - 1 - ((bb << (L - 4)) + (j >> (8 - L)))], p);
         }
     }
     {
@@ -289,11 +298,11 @@ __device__ __forceinline__ void ntt_inv(uint32_t (&v)[VPT], const uint2 *__restr
         const int dj = 8 >> L;
 #pragma unroll
         for (int j = 0; j < VPT; j++)
-            if ((j & dj) == 0) gs_bfly(v[j], v[j + dj], tw[(1 << L) + j / (2 * dj)], p);
+            if ((j & dj) == 0) gs_bfly_neg(v[j], v[j + dj], tw[(2 << L) - 1 - j / (2 * dj)], p);
     }
 }
 
-// Copy the four twiddle tables into shared memory (all threads of the CTA).
+// Copy the two twiddle tables into shared memory (all threads of the CTA).
 // Eight loads are issued before their stores, so a CTA pays about one L2
 // latency per 8 x blockDim 16-byte words instead of one per word.
 __device__ __forceinline__ void load_twiddles(uint32_t *dst, const TwiddleSet *src) {

@@ -29,27 +29,18 @@ void build_twiddles_host(TwiddleSet *h) {
     for (int k = 0; k < 2; k++) {
         const Prime c = prime_of(k);
         const uint64_t p = c.p;
-        const uint64_t psi_inv = powmod_c(psi[k], 4095, p);
-        uint32_t f[D], iv[D], fq[D], ivq[D], rf[D], riv[D], rfq[D], rivq[D];
+        uint32_t f[D], fq[D], rf[D], rfq[D];
         for (uint32_t i = 0; i < (uint32_t)D; i++) {
-            uint32_t e = brev11(i);
-            f[i] = (uint32_t)powmod_c(psi[k], e, p);
-            iv[i] = (uint32_t)powmod_c(psi_inv, e, p);
+            f[i] = (uint32_t)powmod_c(psi[k], brev11(i), p);
             fq[i] = (uint32_t)(((uint64_t)f[i] << 32) / p);      // Shoup companions
-            ivq[i] = (uint32_t)(((uint64_t)iv[i] << 32) / p);
         }
         restride(f, rf);
-        restride(iv, riv);
         restride(fq, rfq);
-        restride(ivq, rivq);
-        for (int i = 0; i < D; i++) {
-            h->t[k][i] = make_uint2(rf[i], rfq[i]);
-            h->t[2 + k][i] = make_uint2(riv[i], rivq[i]);
-        }
+        for (int i = 0; i < D; i++) h->t[k][i] = make_uint2(rf[i], rfq[i]);
     }
 }
 
-// Shared memory of the NTT kernels: 4 twiddle tables + 2 groups x 2 buffers.
+// Shared memory of the NTT kernels: 2 twiddle tables + 2 groups x 2 buffers.
 constexpr int NTT_SMEM_WORDS = TW_WORDS + 2 * 2 * D;
 
 __global__ void __launch_bounds__(256) k_to_ntt(const uint64_t *__restrict__ raw, uint32_t *__restrict__ out,
@@ -88,7 +79,7 @@ __global__ void __launch_bounds__(256) k_from_ntt(const uint32_t *__restrict__ i
         ld16(v, in + ((size_t)i * 2 + g) * D + VPT * t);
 #pragma unroll
         for (int j = 0; j < VPT; j++) v[j] = reduce2(v[j], 2 * c.p) ;
-        ntt_inv(v, tw_of(smem, 2 + g), buf, c, t, 1 + g);
+        ntt_inv(v, tw_of(smem, g), buf, c, t, 1 + g);
 #pragma unroll
         for (int j = 0; j < VPT; j++) xch[g * D + t + GROUP * j] = v[j];
         __syncthreads();
@@ -123,7 +114,7 @@ __global__ void __launch_bounds__(256) k_ntt_planes(uint32_t *__restrict__ a, in
             st16(pl + VPT * t, v);
         } else {
             ld16(v, pl + VPT * t);
-            ntt_inv(v, tw_of(smem, 2 + g), buf, c, t, 1 + g);
+            ntt_inv(v, tw_of(smem, g), buf, c, t, 1 + g);
 #pragma unroll
             for (int j = 0; j < VPT; j++) {
                 uint32_t x = mont_mul(v[j], c.ninv_m, c.p, c.pinv);

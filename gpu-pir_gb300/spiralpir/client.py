@@ -25,7 +25,7 @@ import dataclasses
 
 import numpy as np
 
-from . import ring
+from . import prg, ring
 from .params import D, Q, Q1, Q2, DbShape, SpiralParams, bits_per, delta
 
 SIGMA = 6.4
@@ -71,11 +71,22 @@ class Client:
         self.s_gsw_ntt = ring.to_ntt(ring.signed_to_raw(self.s_gsw))
 
     # -- encryption ------------------------------------------------------
+    def _uniform_rows(self, lead) -> np.ndarray:
+        """Uniform NTT polynomials for row 0 of the next key ciphertexts: the
+        seeded stream (prg.seeded_poly, in key-set order) while a seeded key
+        set is being made, else the negation of the client's generator draw."""
+        if getattr(self, "_seed", None) is None:
+            return ring.neg(_uniform_ntt(self.rng, lead))
+        n = int(np.prod(lead, dtype=np.int64)) if lead else 1
+        out = np.stack([prg.seeded_poly(self._seed, self._seed_next + i) for i in range(n)])
+        self._seed_next += n
+        return out.reshape(tuple(lead) + (2, D))
+
     def _enc(self, m_ntt: np.ndarray) -> np.ndarray:
         """Regev encryption of NTT-form messages (..., 2, D) -> (..., 2 rows, 2, D)."""
         m_ntt = np.asarray(m_ntt, dtype=np.uint64)
         lead = m_ntt.shape[:-2]
-        a = _uniform_ntt(self.rng, lead)
+        a = ring.neg(self._uniform_rows(lead))      # row 0 = -a is the uniform row
         e = ring.to_ntt(ring.signed_to_raw(_gaussian(self.rng, lead + (D,))))
         b = ring.add(ring.add(ring.mul(self.s_ntt, a), e), m_ntt)
         return np.stack((ring.neg(a), b), axis=-3)
@@ -113,7 +124,7 @@ class Client:
         out = np.empty((n, n + 1, t, 2, D), dtype=np.uint64)
         for r in range(n):
             for k in range(t):
-                a = _uniform_ntt(self.rng, ())
+                a = ring.neg(self._uniform_rows(()))
                 out[r, 0, k] = ring.neg(a)
                 for i in range(n):
                     e = ring.to_ntt(ring.signed_to_raw(_gaussian(self.rng, (D,))))
@@ -123,17 +134,26 @@ class Client:
                     out[r, 1 + i, k] = v
         return out.astype(np.uint32)
 
-    def public_keys(self, max_nu1: int, max_nu2: int) -> PublicKeys:
-        """Keys for any database with nu1 <= max_nu1 and nu2 <= max_nu2."""
+    def public_keys(self, max_nu1: int, max_nu2: int, seed: bytes | None = None) -> PublicKeys:
+        """Keys for any database with nu1 <= max_nu1 and nu2 <= max_nu2.
+        With a 32-byte `seed`, row 0 of every key matrix is the seeded stream
+        (prg.seeded_poly), so the server can regenerate it
+        (SpiralGPU.set_client_keys_seeded); the keys are returned in full."""
         p = self.params
         g = max(p.g(a, b) for a in range(1, max_nu1 + 1) for b in range(1, max_nu2 + 1))
         stop = max(p.stop_round(b) for b in range(1, max_nu2 + 1))
-        return PublicKeys(
-            exp_left=self.expansion_keys(g, p.t_exp_left),
-            exp_right=self.expansion_keys(stop + 1, p.t_exp_right),
-            conv=self.conversion_key(),
-            pack=self.packing_keys(),
-        )
+        if seed is not None and len(bytes(seed)) != 32:
+            raise ValueError("the seed is 32 bytes")
+        self._seed, self._seed_next = (bytes(seed), 0) if seed is not None else (None, 0)
+        try:
+            return PublicKeys(
+                exp_left=self.expansion_keys(g, p.t_exp_left),
+                exp_right=self.expansion_keys(stop + 1, p.t_exp_right),
+                conv=self.conversion_key(),
+                pack=self.packing_keys(),
+            )
+        finally:
+            self._seed = None
 
     # -- query -------------------------------------------------------------
     def query_poly(self, shape: DbShape, index: int) -> np.ndarray:

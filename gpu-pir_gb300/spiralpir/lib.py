@@ -19,6 +19,8 @@ LIB_PATH = os.path.join(_HERE, "libspiralpir.so")
 HEADER = os.path.join(os.path.dirname(os.path.dirname(_HERE)), "include", "spiralpir.h")
 
 SP_OK = 0
+SPLIT_AUTO = 127     # sp_set_split_schedule: autotune per batch class
+SPLIT_NONE = -16     # one CTA per item in every narrow launch
 ERRORS = {1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "NOT_FOUND", 5: "DEVICE", 6: "UNSUPPORTED", 7: "IO"}
 
 
@@ -69,6 +71,9 @@ _SIGS = {
     "sp_db_load_ntt": [_P, _I, _P, _I, _I],
     "sp_db_unload": [_P, _I],
     "sp_client_set_keys": [_P, _I, _P, _I, _P, _I, _P, _P],
+    "sp_client_set_keys_seeded": [_P, _I, _P, _P, _I, _P, _I, _P, _P],
+    "sp_set_split_schedule": [_P, _I],
+    "sp_tuning_report": [_P, _P, _U64],
     "sp_client_evict": [_P, _I],
     "sp_answer": [_P, _I, _I, _P, _P, _U64],
     "sp_answer_batch": [_P, _I, ctypes.POINTER(SpRequest)],
@@ -218,6 +223,29 @@ class SpiralGPU:
         conv, pack = as_u64(keys.conv), as_u64(keys.pack)
         _check(self.lib.sp_client_set_keys(self.h, client_id, _ptr(left), left.shape[0], _ptr(right),
                                            right.shape[0], _ptr(conv), _ptr(pack)))
+
+    def set_client_keys_seeded(self, client_id: int, seed: bytes, keys: PublicKeys) -> None:
+        """Register keys whose row 0 (every key matrix) the library expands
+        from `seed` on the device; only the other rows of `keys` are sent."""
+        if len(seed) != 32:
+            raise ValueError("the seed is 32 bytes")
+        sd = np.frombuffer(bytes(seed), dtype=np.uint8).copy()
+        left = as_u64(keys.exp_left[:, 1])
+        right = as_u64(keys.exp_right[:, 1])
+        conv = as_u64(keys.conv[1])
+        pack = as_u64(keys.pack[:, 1:])
+        _check(self.lib.sp_client_set_keys_seeded(self.h, client_id, _ptr(sd), _ptr(left), left.shape[0],
+                                                  _ptr(right), right.shape[0], _ptr(conv), _ptr(pack)))
+
+    def set_split_schedule(self, shift: int) -> None:
+        """Force the narrow launches' split schedule (SPLIT_NONE, or a shift
+        in [-4, 4]) or autotune it per batch class (SPLIT_AUTO, the default)."""
+        _check(self.lib.sp_set_split_schedule(self.h, int(shift)))
+
+    def tuning_report(self) -> str:
+        buf = ctypes.create_string_buffer(1 << 16)
+        _check(self.lib.sp_tuning_report(self.h, buf, len(buf)))
+        return buf.value.decode()
 
     def evict_client(self, client_id: int) -> None:
         _check(self.lib.sp_client_evict(self.h, client_id))

@@ -140,6 +140,23 @@ int sp_db_restore(sp_ctx *ctx, int32_t db_id, const char *path);
 int sp_client_set_keys(sp_ctx *ctx, int32_t client_id, const uint64_t *exp_left, int32_t n_left,
                        const uint64_t *exp_right, int32_t n_right, const uint64_t *conv,
                        const uint64_t *pack);
+/* The same keys with their uniform rows given by a 32-byte seed (the
+ * "public parameters: store the RNG seed as sent, expand the RNG on the GPU"
+ * plan of gpu-pir/optplan.md:88-92): row 0 of every key matrix is
+ * regenerated on the device from `seed` (ChaCha20 block function of
+ * RFC 8439: key = seed, counter = block, nonce = (row-0 polynomial index,
+ * prime index, 0x3153504B); block b gives residues 8b..8b+7, each the 64-bit
+ * word of two consecutive block words reduced mod the prime; polynomials are
+ * numbered left (matrix, column), right, conversion (column), packing
+ * (matrix, column)).  The other rows are passed, uint64 CRT form:
+ *   left_rest  [n_left][t_exp_left][2][D]     (row 1)
+ *   right_rest [n_right][t_exp_right][2][D]   (row 1)
+ *   conv_rest  [2*t_conv][2][D]               (row 1)
+ *   pack_rest  [n][n][t_conv][2][D]           (rows 1..n)
+ * The upload shrinks by one row of each matrix (about half). */
+int sp_client_set_keys_seeded(sp_ctx *ctx, int32_t client_id, const uint8_t *seed, const uint64_t *left_rest,
+                              int32_t n_left, const uint64_t *right_rest, int32_t n_right, const uint64_t *conv_rest,
+                              const uint64_t *pack_rest);
 int sp_client_evict(sp_ctx *ctx, int32_t client_id);
 
 /* ------------------------------------------------------------------ */
@@ -200,6 +217,20 @@ int sp_wait(sp_ctx *ctx, uint64_t ticket, int32_t *status);
 int sp_wait_timed(sp_ctx *ctx, uint64_t ticket, int32_t *status, double *server_ms);
 int sp_serve_stats(sp_ctx *ctx, uint64_t *served, uint64_t *batches, uint64_t *queued);
 
+/* Split schedule of the narrow launches (no counterpart in the reference):
+ * an expansion round, fold level or pack with few items spreads each item
+ * over split = min(SMs / items, cap) CTAs, shifted by the schedule (shift
+ * s: x 2^s, s < 0: / 2^-s; SP_SPLIT_NONE: one CTA per item).  By default
+ * (SP_SPLIT_AUTO) the schedule is autotuned per batch class (ceil(log2 of
+ * the query count), deepest expansion, deepest fold): on a class's first run
+ * every candidate (0, -1, +1, none) runs the whole pipeline on the batch at
+ * hand and the fastest is kept.  Results are identical under every
+ * schedule.  sp_tuning_report writes the multiply-variant choices and the
+ * tuned classes (candidate times, choice) as text lines into buf. */
+#define SP_SPLIT_AUTO 127
+#define SP_SPLIT_NONE (-16)
+int sp_set_split_schedule(sp_ctx *ctx, int32_t shift);
+int sp_tuning_report(sp_ctx *ctx, char *buf, uint64_t len);
 int sp_stats(sp_ctx *ctx, sp_stats_out *out);
 int sp_stats_reset(sp_ctx *ctx);
 /* Time `iters` launches of the first-dimension multiply of db_id on the
