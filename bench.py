@@ -30,6 +30,7 @@ own replica of the database ("replicas only": the path does not shard here).
 from __future__ import annotations
 
 import argparse
+import faulthandler
 import json
 import os
 import subprocess
@@ -219,6 +220,52 @@ def measured_traffic(algo_bytes: float):
     return float(d["traffic_over_algorithmic"]) * algo_bytes
 
 
+def expansion_outputs(p, nu1: int, nu2: int) -> int:
+    """Expansion outputs computed per query (every round's live outputs
+    after the reference's pruning, gpu-pir/expansion.cuh:92-97)."""
+    g, stop, max_bits = p.g(nu1, nu2), p.stop_round(nu2), p.t_gsw * nu2
+    n = 0
+    for r in range(g):
+        for i in range(2 << r):
+            if r > stop and i & 1:
+                continue
+            if r == stop and i & 1 and i // 2 >= max_bits:
+                continue
+            n += 1
+    return n
+
+
+def int_roofline(p, sh, B: int, stages_ms: dict, sm_mhz: float | None) -> dict | None:
+    """Issue-slot roofline of the NTT-bound stages of a B-query batch: warp
+    instructions per fold, per expansion output and per converted polynomial
+    from the ncu capture of a small batch (profiles/int_pipe.json) times the
+    items of this batch, over the stage's CUDA-event time, against the SMs'
+    issue ceiling (4 schedulers x 1 warp instruction per cycle per SM) at the
+    SM clock sampled during the run; the ALU pipe (the busier integer pipe)
+    against its own ceiling."""
+    path = os.path.join(ROOT, "profiles", "int_pipe.json")
+    if not os.path.exists(path) or not sm_mhz:
+        return None
+    with open(path) as f:
+        k = json.load(f)["kernels"]
+    sms = 152
+    issue_peak = sms * 4 * sm_mhz * 1e6
+    folds = B * p.T * ((1 << sh.nu2) - 1)
+    polys = B * p.T * 2 * (1 << sh.nu2)
+    outs = B * expansion_outputs(p, sh.nu1, sh.nu2)
+    out = {"sm_mhz": sm_mhz, "issue_peak_warp_inst_per_s": issue_peak, "source": "profiles/int_pipe.json"}
+    for stage, parts, ms in (("fold", (("k_fold_level<1>", folds), ("k_acc_to_raw", polys)), stages_ms["fold"]),
+                             ("expand", (("k_expand_round<1>", outs),), stages_ms["expand"])):
+        inst = sum(k[name]["warp_inst_per_item"] * n for name, n in parts)
+        alu = sum(k[name]["alu_inst_per_item"] * n for name, n in parts)
+        alu_rate = k[parts[0][0]].get("alu_warp_inst_per_scheduler_cycle_peak") or 0.5
+        achieved = inst / (ms / 1e3)
+        out[stage] = {"items": {name: n for name, n in parts}, "warp_inst": inst, "ms": ms,
+                      "achieved_warp_inst_per_s": achieved, "issue_frac": achieved / issue_peak,
+                      "alu_pipe_frac": alu / (ms / 1e3) / (issue_peak * alu_rate)}
+    return out
+
+
 def make_workload(seed: int = 0, n_queries: int = 64):
     """The 1 GiB database, a seeded client with its public keys, and
     `n_queries` queries for distinct seeded records."""
@@ -358,6 +405,7 @@ def run_gpu(args, rank, world, local):
     t0 = time.perf_counter()
     gpu.load_db(1, recs, sh.nu1, sh.nu2)
     load_s = time.perf_counter() - t0
+    progress("headline")
     # correctness of the measured configuration
     resp0 = gpu.answer(1, 1, queries[0])
     ok = bool(np.array_equal(cl.decode(resp0), recs[idx[0]]))
@@ -396,7 +444,8 @@ def run_gpu(args, rank, world, local):
         mul_ms = gpu.time_db_mul(1, batch, max(args.steps, 5))
     # end to end through the public API (host buffers)
     lat = []
-    out = np.empty(gpu.response_bytes, dtype=np.uint8)
+    resp_bytes = int(gpu.response_bytes)
+    out = np.empty(resp_bytes, dtype=np.uint8)
     with clocks.window():
         t_e2e = time.perf_counter()
         for i in range(args.steps):
@@ -407,6 +456,7 @@ def run_gpu(args, rank, world, local):
     clk = clocks.summary(clocks.windows)
     if barrier:
         barrier()
+    progress("batched")
     # batched answering (B queries per pipeline run), same database; every
     # batched response is compared byte for byte with the same query
     # answered alone and decoded
@@ -454,8 +504,17 @@ def run_gpu(args, rank, world, local):
                                     "frac": flops / (tc_ms / 1e3) / 1e12 / tpeak, "peak_source": tkind,
                                     "flops_per_launch": flops, "launch_ms": tc_ms}
             entry["clocks"] = clocks.summary(clocks.windows[-2:])
+            entry["roofline_int"] = int_roofline(p, sh, B, entry["stages_ms"],
+                                                 (entry["clocks"] or clk or {}).get("sm_mhz"))
             batched.append(entry)
         gpu2.close()
+    other = None
+    if world == 1 and not args.no_other:
+        gpu.close()
+        gpu = None
+        n_win = len(clocks.windows)
+        other = bench_other(p, cl, keys, recs, clocks, with_8gib=not args.skip_8gib)
+        other["clocks"] = clocks.summary(clocks.windows[n_win:])
     clocks.stop()
 
     value = batch * 1e3 / ms * world
@@ -472,7 +531,7 @@ def run_gpu(args, rank, world, local):
             "scaling": "weak", "vs_baseline": None, "dtype": "u32 (exact modular)",
             "data": "synthetic (seeded records, client and query)", "config": WORKLOAD,
             "e2e": {"value": args.steps / e2e_s * world, "unit": UNIT, "h2d_bytes_per_step": 4 * 2048 * 8,
-                    "d2h_bytes_per_step": int(gpu.response_bytes),
+                    "d2h_bytes_per_step": resp_bytes,
                     "p50_ms": lat_ms[len(lat_ms) // 2], "p99_ms": lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))]},
             "roofline": {"bound": "hbm", "kernel": "k_db_mul", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
@@ -482,8 +541,12 @@ def run_gpu(args, rank, world, local):
                           ("ms_expand", "ms_convert", "ms_db_mul", "ms_fold", "ms_pack", "ms_total")},
             "gpu_launches": int(st["launches"]), "launches_per_answer": launches_per_answer,
             "batched": batched, "clocks": clk, "db_load_s": load_s, "decoded_ok": ok}
-    gpu.close()
+    if other is not None:
+        line["other_configs"] = other
+    if gpu is not None:
+        gpu.close()
     if rank == 0:
+        progress("CPU oracle")
         orc = CpuOracle(p, sh, recs, keys)
         line["cpu_baseline"] = cpu_baseline(orc, queries[0], resp0)
         del orc
@@ -503,6 +566,7 @@ def run_gpu(args, rank, world, local):
 
 
 def main():
+    faulthandler.enable()     # a native crash prints the Python stack on stderr
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=50)
@@ -510,13 +574,9 @@ def main():
     ap.add_argument("--impl", choices=["gpu", "reference"], default="gpu")
     ap.add_argument("--batch", type=int, default=1, help="queries per step (1 = plain single-query path)")
     ap.add_argument("--batched", type=int, default=32, help="also measure a B-query batch (0 to skip)")
-    ap.add_argument("--suite", action="store_true", help="run the other workloads instead (uneven batches, "
-                    "8 GiB database, serving)")
-    ap.add_argument("--skip-8gib", action="store_true", help="suite without the 8 GiB database")
+    ap.add_argument("--no-other", action="store_true", help="skip the uneven-batch, 8 GiB and serving workloads")
+    ap.add_argument("--skip-8gib", action="store_true", help="the other workloads without the 8 GiB database")
     args = ap.parse_args()
-    if args.suite:
-        run_suite(args)
-        return
     if args.warmup < 3:
         args.warmup = 3
     rank, world, local = dist_info()
@@ -529,182 +589,235 @@ def main():
 
 
 
-# --------------------------------------------------------------- suite
-def run_suite(args) -> None:
-    """The other workloads of the answer path, one JSON line each:
-    uneven batches (1 GiB + 64 MiB databases, B in 8/32/64), the 8 GiB
-    database (64 GiB device image) single and B = 16, and the serving loop
-    (three resident databases, 256 clients under an HBM budget with LRU key
-    eviction, seeded Poisson arrivals at swept rates)."""
+# ------------------------------------------------- the other workloads
+# Each returns a dict for the JSON line; bench_other() runs them after the
+# headline measurement and records a failing one as {"error": ...} instead
+# of losing the whole line.
+
+def bench_uneven(p, cl, keys, recs1g, clocks) -> dict:
+    """Uneven batches: B in {8, 32, 64} queries alternating between the
+    1 GiB database (nu1 = 9, nu2 = 8) and a 64 MiB database (nu1 = 8,
+    nu2 = 5), answered in one pipeline run (one multiply launch per
+    database).  Every batched response is compared byte for byte with the
+    same query answered alone, and decoded."""
     from spiralpir import client as C
     from spiralpir import params as P
-    from spiralpir.lib import SpiralError, SpiralGPU
-    from spiralpir.serving import Server, poisson_load
+    from spiralpir.lib import SpiralGPU
 
-    import dataclasses
-
-    p = P.PARAMS
-    # The 8 GiB database (nu2 = 11: 11 fold levels, GSW bits expanded over 8
-    # rounds) leaves too little noise margin with 7-bit digits on the
-    # GSW-bit branch of the expansion (about 1 decode in 240 fails); its runs
-    # use t_exp_right = 16 (4-bit digits), the first-dimension branch keeps 8.
-    p8 = dataclasses.replace(p, t_exp_right=16)
-    out = {"suite": True}
-    key_sets = [C.Client(p, seed=100 + k) for k in range(8)]
-    keys = [cl.public_keys(9, 11) for cl in key_sets]
-    key_sets8 = [C.Client(p8, seed=100 + k) for k in range(8)]
-    keys8 = [cl.public_keys(9, 11) for cl in key_sets8]
-    shapes = {"64MiB": P.SHAPE_64MIB, "1GiB": P.SHAPE_1GIB, "8GiB": P.SHAPE_8GIB}
-    recs = {}
-    t0 = time.perf_counter()
-    recs["64MiB"] = C.random_records(P.SHAPE_64MIB, p, seed=201)
-    recs["1GiB"] = C.random_records(P.SHAPE_1GIB, p, seed=202)
-    if not args.skip_8gib:
-        recs["8GiB"] = C.random_records(P.SHAPE_8GIB, p, seed=203)
-    gen_s = time.perf_counter() - t0
+    shapes = {1: P.SHAPE_1GIB, 2: P.SHAPE_64MIB}
+    recs = {1: recs1g, 2: C.random_records(P.SHAPE_64MIB, p, seed=201)}
     rng = np.random.default_rng(7)
+    out = []
+    with SpiralGPU(p, max_batch=64) as g:
+        g.set_client_keys(1, keys)
+        for db, sh in shapes.items():
+            g.load_db(db, recs[db], sh.nu1, sh.nu2)
+        for B in (8, 32, 64):
+            reqs, idx = [], []
+            for s in range(B):
+                db = 1 + s % 2
+                i = int(rng.integers(0, shapes[db].num_records))
+                reqs.append((1, db, cl.query(shapes[db], i)))
+                idx.append(i)
+            # staged (device-resident) timing: slots grouped by database
+            order = sorted(range(B), key=lambda s: reqs[s][1])
+            for slot, s in enumerate(order):
+                g.stage_query(slot, *reqs[s])
+            g.time_staged(B, 2)
+            with clocks.window():
+                ms = g.time_staged(B, 5)
+            g.stats_reset()
+            g.run_staged(B)
+            st = g.stats()
+            batch = g.answer_batch(reqs)
+            alone = [g.answer(*r) for r in reqs]
+            eq = sum(bool(np.array_equal(a, b)) for a, b in zip(batch, alone))
+            dec = sum(bool(np.array_equal(cl.decode(r), recs[reqs[s][1]][idx[s]])) for s, r in enumerate(batch))
+            out.append({"B": B, "mix": "1GiB:64MiB = 1:1", "ms_per_batch": ms, "queries_per_s": B / ms * 1e3,
+                        "stages_ms": {k[3:]: st[k] for k in ("ms_expand", "ms_convert", "ms_db_mul", "ms_fold",
+                                                            "ms_pack", "ms_total")},
+                        "bytes_equal_single": eq, "decoded_ok": dec})
+    return {"batches": out}
 
-    def query_for(k, name, ks=None):
-        sh = shapes[name]
-        idx = int(rng.integers(0, sh.num_records))
-        return (ks or key_sets)[k].query(sh, idx), idx
 
-    # uneven batches: 1 GiB and 64 MiB queries mixed in one batch
-    g = SpiralGPU(p, max_batch=64)
-    for k in range(8):
-        g.set_client_keys(k, keys[k])
-    g.load_db(1, recs["1GiB"], 9, 8)
-    g.load_db(2, recs["64MiB"], 8, 5)
-    single = []
-    for name, db in (("1GiB", 1), ("64MiB", 2)):
-        q, idx = query_for(0, name)
-        g.answer(0, db, q)
+def bench_8gib(p, recs8, clocks) -> dict:
+    """The 8 GiB database (nu1 = 9, nu2 = 11: 2^20 records, a 56 GiB packed
+    image): one query per pipeline run and B = 16 in one run, the multiply's
+    HBM fraction, and the multiply variants' time per query as B grows (the
+    arithmetic-intensity crossover).  The B = 16 responses are compared with
+    the same queries answered alone; all are decoded (decode failures at this
+    depth come from the parameters' noise budget, not from the arithmetic,
+    which is bit-exact)."""
+    from spiralpir import client as C
+    from spiralpir import params as P
+    from spiralpir.lib import SpiralGPU
+
+    sh = P.SHAPE_8GIB
+    cl = C.Client(p, seed=301)
+    keys = cl.public_keys(sh.nu1, sh.nu2)
+    rng = np.random.default_rng(302)
+    idx = [int(x) for x in rng.choice(sh.num_records, size=16, replace=False)]
+    qs = [cl.query(sh, i) for i in idx]
+    peak, _ = measured_peaks()
+    with SpiralGPU(p, max_batch=16) as g:
+        g.set_client_keys(1, keys)
         t1 = time.perf_counter()
-        for _ in range(5):
-            r = g.answer(0, db, q)
-        single.append({"db": name, "e2e_ms": (time.perf_counter() - t1) / 5 * 1e3,
-                       "ok": bool(np.array_equal(key_sets[0].decode(r), recs[name][idx]))})
-    out["single"] = single
-    uneven = []
-    for B in (8, 32, 64):
-        reqs, checks = [], []
-        for s in range(B):
-            name, db = ("1GiB", 1) if s % 2 == 0 else ("64MiB", 2)
-            k = s % 8
-            q, idx = query_for(k, name)
-            reqs.append((k, db, q))
-            checks.append((k, name, idx))
-        # staged (device-resident) timing: slots must be in database order
-        order = sorted(range(B), key=lambda s: reqs[s][1])
-        for slot, s in enumerate(order):
-            g.stage_query(slot, reqs[s][0], reqs[s][1], reqs[s][2])
-        g.time_staged(B, 1)
-        ms = g.time_staged(B, 3)
-        g.stats_reset()
-        g.run_staged(B)
-        st = g.stats()
-        resp = g.answer_batch(reqs)
-        ok = all(np.array_equal(key_sets[k].decode(r), recs[name][idx]) for r, (k, name, idx) in zip(resp, checks))
-        uneven.append({"B": B, "mix": "1GiB:64MiB = 1:1", "ms_per_batch": ms, "queries_per_s": B / ms * 1e3,
-                       "stages_ms": {k[3:]: st[k] for k in ("ms_expand", "ms_convert", "ms_db_mul", "ms_fold",
-                                                           "ms_pack", "ms_total")},
-                       "decoded_ok": ok})
-    out["uneven_batches"] = uneven
-    print(json.dumps({"suite": "uneven_batches", "single": single, "uneven_batches": uneven}), flush=True)
-    g.close()
-
-    # 8 GiB database: 2^20 records, 56 GiB device image
-    if not args.skip_8gib:
-        g = SpiralGPU(p8, max_batch=16)
-        g.set_client_keys(0, keys8[0])
-        t1 = time.perf_counter()
-        g.load_db(3, recs["8GiB"], 9, 11)
+        g.load_db(1, recs8, sh.nu1, sh.nu2)
         load_s = time.perf_counter() - t1
-        q, idx = query_for(0, "8GiB", key_sets8)
-        r = g.answer(0, 3, q)
-        ok = bool(np.array_equal(key_sets8[0].decode(r), recs["8GiB"][idx]))
-        g.stage_query(0, 0, 3, q)
+        alone = [g.answer(1, 1, q) for q in qs]
+        g.stage_query(0, 1, 1, qs[0])
         g.time_staged(1, 1)
-        ms1 = g.time_staged(1, 3)
-        mul = g.time_db_mul(3, 1, 3)
-        img = (1 << 20) * 4 * 2048 * 7   # packed image: 7 bytes per coefficient (two 28-bit residues)
-        abytes = img + 512 * 2048 * 16 + 4 * 2048 * 4 * 2048 * 4
+        with clocks.window():
+            ms1 = g.time_staged(1, 3)
+            mul = g.time_db_mul(1, 1, 3)
+        img = sh.num_records * p.T * 2048 * 7
+        abytes = img + sh.rows * 2048 * 16 + p.T * sh.cols * 4 * 2048 * 4
         for s in range(16):
-            g.stage_query(s, 0, 3, q)
+            g.stage_query(s, 1, 1, qs[s])
         g.time_staged(16, 1)
-        ms16 = g.time_staged(16, 2)
-        ok16 = all(np.array_equal(key_sets8[0].decode(g.fetch_response(s)), recs["8GiB"][idx]) for s in range(16))
-        peak, _ = measured_peaks()
-        # arithmetic-intensity crossover of the first-dimension multiply: time
-        # per query of each variant as B grows (B queries share one image
-        # pass; 0.5 multiply-add per image byte per query)
-        macs_q = (1 << 20) * 4 * 2048 * 2 * 2
-        per_q_bytes = 512 * 2048 * 16 + 4 * 2048 * 4 * 2048 * 4
+        with clocks.window():
+            ms16 = g.time_staged(16, 2)
+        eq = sum(bool(np.array_equal(g.fetch_response(s), alone[s])) for s in range(16))
+        dec = sum(bool(np.array_equal(cl.decode(alone[s]), recs8[idx[s]])) for s in range(16))
+        macs_q = sh.num_records * p.T * 2048 * 2 * 2
+        per_q_bytes = sh.rows * 2048 * 16 + p.T * sh.cols * 4 * 2048 * 4
         crossover = []
-        for variant, bs in ((1, (1,)), (2, (2, 4, 8, 16)), (3, (2, 4, 8, 16))):   # batched variants need B >= 2
+        for variant, bs in ((1, (1,)), (2, (2, 8, 16)), (3, (2, 4, 8, 16))):
             g.set_db_mul_variant(variant)
             for B in bs:
-                ms = g.time_db_mul(3, B, 2)
+                ms = g.time_db_mul(1, B, 2)
                 crossover.append({"variant": variant, "B": B, "ms": ms, "ms_per_query": ms / B,
                                   "gbs": (img + B * per_q_bytes) / ms / 1e6, "tmacs": B * macs_q / ms / 1e9})
         g.set_db_mul_variant(0)
-        out["db_8gib"] = {"t_exp_right": 16, "load_s": load_s, "decoded_ok": ok, "single_ms": ms1, "single_qps": 1e3 / ms1,
-                          "db_mul_ms": mul, "db_mul_gbs": abytes / mul / 1e6, "db_mul_frac": abytes / mul / 1e6 / peak,
-                          "B16_ms": ms16, "B16_qps": 16e3 / ms16, "B16_decoded_ok": ok16,
-                          "db_mul_crossover": crossover}
-        print(json.dumps({"suite": "db_8gib", **out["db_8gib"]}), flush=True)
-        g.close()
+    return {"t_exp": [p.t_exp_left, p.t_exp_right], "load_s": load_s, "single_ms": ms1, "single_qps": 1e3 / ms1,
+            "db_mul_ms": mul, "db_mul_gbs": abytes / mul / 1e6, "db_mul_frac": abytes / mul / 1e6 / peak,
+            "B16_ms": ms16, "B16_qps": 16e3 / ms16, "B16_bytes_equal_single": eq, "decoded_ok": dec,
+            "queries": 16, "db_mul_crossover": crossover}
 
-    # serving: three resident databases, 256 clients, HBM budget with LRU eviction
-    names = ["64MiB", "1GiB"] + ([] if args.skip_8gib else ["8GiB"])
+
+def bench_serving(p, recs_by_name, clocks, rates=(250.0, 500.0, 1000.0, 2000.0), n_req=400,
+                  n_warm=300) -> dict:
+    """Serving: the 64 MiB, 1 GiB and 8 GiB databases resident, 256 clients
+    (32 distinct key sets) under an HBM budget that holds about 120 clients'
+    keys, so registering each rate's 96 active clients evicts the least
+    recently used.  Seeded Poisson arrivals with a uniform mix over the
+    databases go (1) to the continuous-batching server (one server for all
+    rates, after a warm-up run that lets the autotuner see the batch
+    classes) and (2) to the plain single-query loop (one sp_answer at a
+    time); both report achieved queries/s and p50/p99 latency.  The server's
+    responses are compared byte for byte with the single-query loop's (the
+    same queries answered alone) and decoded."""
+    from spiralpir import client as C
+    from spiralpir import params as P
+    from spiralpir.lib import SpiralGPU
+    from spiralpir.serving import Server, poisson_load, single_query_loop
+
+    names = list(recs_by_name)
+    shapes = {"64MiB": P.SHAPE_64MIB, "1GiB": P.SHAPE_1GIB, "8GiB": P.SHAPE_8GIB}
     ids = {n: i + 1 for i, n in enumerate(names)}
-    key_bytes = sum(a.nbytes for a in (keys8[0].exp_left, keys8[0].exp_right, keys8[0].conv, keys8[0].pack))
+    key_sets = [C.Client(p, seed=400 + k) for k in range(32)]
+    keys = [cl.public_keys(9, 11) for cl in key_sets]
+    key_bytes = sum(a.nbytes for a in (keys[0].exp_left, keys[0].exp_right, keys[0].conv, keys[0].pack))
+    rng = np.random.default_rng(401)
 
-    def serving_ctx(budget):
-        g = SpiralGPU(p8, max_batch=32, hbm_budget_bytes=budget)
+    def workload(n):
+        active = [int(x) for x in rng.choice(256, size=96, replace=False)]
+        reqs, checks = [], []
+        for _ in range(n):
+            cid = active[int(rng.integers(0, len(active)))]
+            name = names[int(rng.integers(0, len(names)))]
+            i = int(rng.integers(0, shapes[name].num_records))
+            reqs.append((cid, ids[name], key_sets[cid % 32].query(shapes[name], i)))
+            checks.append((cid, name, i))
+        return active, reqs, checks
+
+    warm = workload(n_warm)
+    runs = [workload(n_req) for _ in rates]
+
+    def ctx(budget):
+        g = SpiralGPU(p, max_batch=32, hbm_budget_bytes=budget)
         for n in names:
-            g.load_db(ids[n], recs[n], shapes[n].nu1, shapes[n].nu2)
+            g.load_db(ids[n], recs_by_name[n], shapes[n].nu1, shapes[n].nu2)
         for k in range(8):
-            g.set_client_keys(k, keys8[k])
-        srv = Server(g, lanes=2)      # reserves both lanes' workspace
-        return g, srv
+            g.set_client_keys(k, keys[k])
+        return g
 
-    g, srv = serving_ctx(0)
+    g = ctx(0)
+    srv = Server(g, lanes=2)          # reserves both lanes' workspace
     used = g.hbm_used()
     srv.stop()
     g.close()
-    budget = used + 120 * key_bytes          # room for ~128 clients' keys; 256 share it by LRU
-    g, srv = serving_ctx(budget)
-    serving, registered = [], 0
-    for rate in (250.0, 500.0, 1000.0, 2000.0, 4000.0):
-        active = rng.choice(256, size=96, replace=False)
-        for cid in active:               # registering evicts the least recently used clients
-            g.set_client_keys(int(cid), keys8[int(cid) % 8])
+    budget = used + 120 * key_bytes
+    g = ctx(budget)
+    registered = 0
+
+    def register(active):
+        nonlocal registered
+        for cid in active:            # registering evicts the least recently used clients
+            g.set_client_keys(cid, keys[cid % 32])
             registered += 1
-        n_req = int(min(600, max(200, rate * 0.5)))
-        reqs, checks = [], []
-        for _ in range(n_req):
-            cid = int(active[int(rng.integers(0, len(active)))])
-            name = names[int(rng.integers(0, len(names)))]
-            q, idx = query_for(cid % 8, name, key_sets8)
-            reqs.append((cid, ids[name], q))
-            checks.append((cid, name, idx))
-        res = poisson_load(srv, reqs, rate_qps=rate, seed=int(rate))
+
+    served = []
+    with Server(g, lanes=2) as srv:
+        register(warm[0])
+        poisson_load(srv, warm[1], rate_qps=max(rates), seed=1)
+        for rate, (active, reqs, _) in zip(rates, runs):
+            register(active)
+            with clocks.window():
+                served.append(poisson_load(srv, reqs, rate_qps=rate, seed=int(rate)))
+        st = srv.stats()
+    rows = []
+    for rate, (active, reqs, checks), res in zip(rates, runs, served):
+        register(active)
+        with clocks.window():
+            plain = single_query_loop(g, reqs, rate_qps=rate, seed=int(rate))
+        out, alone = res.pop("responses"), plain.pop("responses")
+        res["bytes_equal_single"] = sum(bool(np.array_equal(a, b)) for a, b in zip(out, alone))
         wrong = {}
-        for r, (cid, name, idx) in zip(res.pop("responses"), checks):
-            if not np.array_equal(key_sets8[cid % 8].decode(r), recs[name][idx]):
+        for r, (cid, name, i) in zip(out, checks):
+            if not np.array_equal(key_sets[cid % 32].decode(r), recs_by_name[name][i]):
                 wrong[name] = wrong.get(name, 0) + 1
-        res["decoded_ok"] = not wrong
-        if wrong:
-            res["wrong_by_db"] = wrong
-        serving.append(res)
-    st = srv.stats()
-    srv.stop()
-    out["serving"] = {"t_exp_right": 16, "dbs": names, "clients": 256, "hbm_budget_bytes": budget, "key_bytes_per_client": key_bytes,
-                      "client_registrations": registered, "lanes": 2, "max_batch": 32, "rates": serving,
-                      "batches": st["batches"], "served": st["served"]}
+        res["decode_failures_by_db"] = wrong
+        rows.append({"batching": res, "single_query_loop": plain})
     g.close()
-    print(json.dumps({"suite": "serving", **out["serving"], "record_gen_s": gen_s}), flush=True)
+    return {"dbs": names, "clients": 256, "distinct_key_sets": 32, "hbm_budget_bytes": budget,
+            "key_bytes_per_client": key_bytes, "client_registrations": registered, "lanes": 2, "max_batch": 32,
+            "requests_per_rate": n_req, "warmup_requests": n_warm, "batches": st["batches"], "rates": rows}
+
+
+def progress(msg: str) -> None:
+    """A progress note on stderr (the JSON line goes to stdout)."""
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
+def bench_other(p, cl, keys, recs1g, clocks, with_8gib: bool = True) -> dict:
+    """Configs beyond the headline: uneven batches, the 8 GiB database and
+    the serving loop (each guarded: an error is recorded, not raised)."""
+    from spiralpir import client as C
+    from spiralpir import params as P
+
+    out = {}
+    t0 = time.perf_counter()
+    progress("uneven batches")
+    try:
+        out["uneven_batches"] = bench_uneven(p, cl, keys, recs1g, clocks)
+    except Exception as e:  # noqa: BLE001 - recorded in the line
+        out["uneven_batches"] = {"error": repr(e)}
+    recs = {"64MiB": C.random_records(P.SHAPE_64MIB, p, seed=203), "1GiB": recs1g}
+    if with_8gib:
+        progress("8 GiB database")
+        try:
+            recs["8GiB"] = C.random_records(P.SHAPE_8GIB, p, seed=204)
+            out["db_8gib"] = bench_8gib(p, recs["8GiB"], clocks)
+        except Exception as e:  # noqa: BLE001
+            out["db_8gib"] = {"error": repr(e)}
+    progress("serving")
+    try:
+        out["serving"] = bench_serving(p, recs, clocks)
+    except Exception as e:  # noqa: BLE001
+        out["serving"] = {"error": repr(e)}
+    out["seconds"] = time.perf_counter() - t0
+    return out
 
 
 if __name__ == "__main__":

@@ -8,7 +8,9 @@ bytes are written.
 
 `poisson_load` drives a Server with seeded Poisson arrivals and reports
 throughput and server-side latency percentiles (arrival -> response ready,
-timed by the library: sp_wait_timed).
+timed by the library: sp_wait_timed).  `single_query_loop` serves the same
+arrivals with the plain single-query path (one sp_answer at a time, first
+come first served), the baseline the batching server is compared with.
 """
 from __future__ import annotations
 
@@ -114,4 +116,30 @@ def poisson_load(server: Server, requests: list, rate_qps: float, seed: int = 0)
             "mean_ms": float(lat.mean()), "n": len(requests), "responses": outs}
 
 
-__all__ = ["Server", "Ticket", "poisson_load", "threading"]
+def single_query_loop(gpu: SpiralGPU, requests: list, rate_qps: float, seed: int = 0) -> dict:
+    """The plain single-query server under the arrivals of poisson_load with
+    the same seed: requests are answered one at a time in arrival order
+    through sp_answer; latency is arrival -> response returned (host clock)."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate_qps, size=len(requests))
+    arrivals = np.cumsum(gaps)
+    out = np.empty(gpu.response_bytes, dtype=np.uint8)
+    outs, lat = [], []
+    t0 = time.perf_counter()
+    for (cid, did, q), a in zip(requests, arrivals):
+        while True:
+            now = time.perf_counter() - t0
+            if now >= a:
+                break
+            time.sleep(min(a - now, 0.0005))
+        gpu.answer(cid, did, q, out=out)
+        lat.append((time.perf_counter() - t0 - a) * 1e3)
+        outs.append(out.copy())
+    t_end = time.perf_counter() - t0
+    lat = np.array(lat)
+    return {"offered_qps": rate_qps, "achieved_qps": len(requests) / t_end,
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "n": len(requests), "responses": outs}
+
+
+__all__ = ["Server", "Ticket", "poisson_load", "single_query_loop", "threading"]

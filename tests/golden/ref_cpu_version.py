@@ -11,6 +11,8 @@ Reads <work dir>/in.npz and writes <work dir>/out.npz.  Inputs:
   fold_in  uint64 (4, 2, D) raw, fold_keys / fold_keys_neg uint64
            (2, 2, 16, 2, D) in the golden-vector file layout; output fold_out
            uint64 (2, D) = fold_all_ciphertexts (cpu_version/folding.py:45-50)
+Every output also gets its wall time in seconds (`<name>_s`, one core: the
+model is pure Python), the reference's own CPU timing of these stages.
 The reference code is used exactly as shipped (its fixture parameters
 V2 = 2, T_GSW = 8); it reads its inputs through its own loaders
 (cpu_version/testing.py:61-114) from files written here in the golden-vector
@@ -20,6 +22,7 @@ import contextlib
 import io
 import os
 import sys
+import time
 
 sys.dont_write_bytecode = True
 
@@ -39,19 +42,23 @@ def main(ref_dir: str, work: str) -> None:
     primes = [(rparams.Q1, rparams.Q1_MONT, rntt.q1_twiddles, rntt.q1_inv_twiddles),
               (rparams.Q2, rparams.Q2_MONT, rntt.q2_twiddles, rntt.q2_inv_twiddles)]
     if "ntt_in" in inp:
+        t0 = time.perf_counter()
         a = inp["ntt_in"]
         res = np.empty_like(a)
         for i in range(a.shape[0]):
             for k, (q, qm, tw, _) in enumerate(primes):
                 res[i, k] = rntt.gpu_ntt_256([int(x) for x in a[i, k]], q, qm, tw, True)
         out["ntt_out"] = res
+        out["ntt_out_s"] = time.perf_counter() - t0
     if "intt_in" in inp:
+        t0 = time.perf_counter()
         a = inp["intt_in"]
         res = np.empty_like(a)
         for i in range(a.shape[0]):
             for k, (q, qm, _, itw) in enumerate(primes):
                 res[i, k] = rntt.gpu_intt_256([int(x) for x in a[i, k]], q, qm, itw, True)
         out["intt_out"] = res
+        out["intt_out_s"] = time.perf_counter() - t0
     if "fold_in" in inp:
         fin = os.path.join(work, "fold_in.dat")
         fk = os.path.join(work, "fold_keys.dat")
@@ -64,7 +71,9 @@ def main(ref_dir: str, work: str) -> None:
             cts = testing.load_polys(fin, False)
             keys = testing.load_polys(fk, True, 2 * t, True, True, True)
             keys_neg = testing.load_polys(fkn, True, 2 * t, True, True, True)
+            t0 = time.perf_counter()
             folding.fold_all_ciphertexts(cts, keys, keys_neg)
+            out["fold_out_s"] = time.perf_counter() - t0
         ct = cts[0]
         res = np.empty((2, len(ct.a.crt_0.data)), dtype=np.uint64)
         for r, poly in enumerate((ct.a, ct.as_e)):
