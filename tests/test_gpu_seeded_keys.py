@@ -8,6 +8,7 @@ import pytest
 
 from spiralpir import client as C
 from spiralpir import params as P
+from spiralpir import wire
 from spiralpir.lib import SpiralGPU
 
 pytestmark = pytest.mark.gpu
@@ -48,3 +49,21 @@ def test_seeded_keys_with_a_wrong_seed_do_not_decode():
         assert not np.array_equal(cl.decode(r), recs[5])
         with pytest.raises(ValueError):
             gpu.set_client_keys_seeded(2, b"short", keys)
+
+
+def test_seeded_keys_over_the_wire():
+    """Client -> server messages (seeded keys, query) and the response back,
+    through the wire format; the record decodes."""
+    p, sh = P.PARAMS, P.SHAPE_8MIB
+    seed = bytes(range(100, 132))
+    cl = C.Client(p, seed=75)
+    recs = C.random_records(sh, p, seed=76)
+    key_msg = wire.encode_seeded_keys(p, seed, cl.public_keys(sh.nu1, sh.nu2, seed=seed))
+    query_msg = wire.encode_query(p, sh.nu1, sh.nu2, cl.query(sh, 321))
+    with SpiralGPU(p) as gpu:
+        gpu.load_db(1, recs, sh.nu1, sh.nu2)
+        s, keys = wire.decode_seeded_keys(p, key_msg)
+        gpu.set_client_keys_seeded(9, s, keys)
+        _, _, q = wire.decode_query(p, query_msg)
+        resp_msg = wire.encode_response(p, gpu.answer(9, 1, q))
+    assert np.array_equal(cl.decode(wire.decode_response(p, resp_msg)), recs[321])
