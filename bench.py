@@ -702,8 +702,8 @@ def bench_serving(p, recs_by_name, clocks, rates=(250.0, 500.0, 1000.0, 2000.0),
     keys, so registering each rate's 96 active clients evicts the least
     recently used.  Seeded Poisson arrivals with a uniform mix over the
     databases go (1) to the continuous-batching server (one server for all
-    rates, after a warm-up run that lets the autotuner see the batch
-    classes) and (2) to the plain single-query loop (one sp_answer at a
+    rates, after warm-up runs at the lowest and highest rate that let the
+    autotuner see the batch classes) and (2) to the plain single-query loop (one sp_answer at a
     time); both report achieved queries/s and p50/p99 latency.  The server's
     responses are compared byte for byte with the single-query loop's (the
     same queries answered alone) and decoded."""
@@ -731,7 +731,7 @@ def bench_serving(p, recs_by_name, clocks, rates=(250.0, 500.0, 1000.0, 2000.0),
             checks.append((cid, name, i))
         return active, reqs, checks
 
-    warm = workload(n_warm)
+    warm = [workload(n_warm // 2), workload(n_warm // 2)]
     runs = [workload(n_req) for _ in rates]
 
     def ctx(budget):
@@ -759,8 +759,11 @@ def bench_serving(p, recs_by_name, clocks, rates=(250.0, 500.0, 1000.0, 2000.0),
 
     served = []
     with Server(g, lanes=2) as srv:
-        register(warm[0])
-        poisson_load(srv, warm[1], rate_qps=max(rates), seed=1)
+        # warm-up at the lowest and the highest rate: the batch classes of
+        # both are tuned before the measured runs
+        for (active, reqs, _), rate in zip(warm, (min(rates), max(rates))):
+            register(active)
+            poisson_load(srv, reqs, rate_qps=rate, seed=1)
         for rate, (active, reqs, _) in zip(rates, runs):
             register(active)
             with clocks.window():

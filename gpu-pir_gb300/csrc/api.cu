@@ -662,8 +662,8 @@ cudaError_t enqueue_inputs(Lane &L, int nq, cudaStream_t st) {
 // Autotuner of the narrow launches' split schedule (answer.cuh
 // shifted_split).  The pipeline is idempotent from its staged inputs, so each
 // candidate schedule runs it (on the batch at hand, after one untimed run),
-// timed between the first and the last stage event as the better of two
-// runs; the fastest is kept for the batch class
+// timed between the first and the last stage event; the fastest is kept for
+// the batch class
 // `key` = (ceil(log2 nq), deepest expansion, deepest fold); ties favour the
 // rule, shift 0.  Every schedule gives identical residues.  The class and the
 // candidate times go to the tuning log (sp_tuning_report).
@@ -675,19 +675,15 @@ int tune_split(sp_ctx *c, Lane &L, const std::vector<int64_t> &key, Enqueue &enq
     std::string msg = "plan class nq<=" + std::to_string(1ll << key[0]) + " g=" + std::to_string(key[1]) +
                       " nu2=" + std::to_string(key[2]) + ":";
     // one untimed run first (caches, lazily loaded kernels), then each
-    // candidate timed as the better of two runs
+    // candidate timed once
     *shift = 0;
     CU(enqueue(false));
     for (int cand : cands) {
         *shift = cand;
         float ms = 0;
-        for (int rep = 0; rep < 2; rep++) {
-            CU(enqueue(false));
-            CU(cudaEventSynchronize(L.ev[5]));
-            float m = 0;
-            CU(cudaEventElapsedTime(&m, L.ev[0], L.ev[5]));
-            ms = rep ? std::min(ms, m) : m;
-        }
+        CU(enqueue(false));
+        CU(cudaEventSynchronize(L.ev[5]));
+        CU(cudaEventElapsedTime(&ms, L.ev[0], L.ev[5]));
         msg += " shift " + (cand == SPLIT_NONE ? std::string("none") : std::to_string(cand)) + " " +
                std::to_string(ms).substr(0, 6) + " ms;";
         if (cand == 0 || ms < best_ms * 0.99f) {

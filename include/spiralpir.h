@@ -223,8 +223,8 @@ int sp_serve_stats(sp_ctx *ctx, uint64_t *served, uint64_t *batches, uint64_t *q
  * s: x 2^s, s < 0: / 2^-s; SP_SPLIT_NONE: one CTA per item).  By default
  * (SP_SPLIT_AUTO) the schedule is autotuned per batch class (ceil(log2 of
  * the query count), deepest expansion, deepest fold): on a class's first run
- * every candidate (0, -1, +1, none) runs the whole pipeline on the batch at
- * hand and the fastest is kept.  Results are identical under every
+ * the pipeline runs once untimed, then once per candidate (0, -1, +1, none)
+ * on the batch at hand, and the fastest is kept.  Results are identical under every
  * schedule.  sp_tuning_report writes the multiply-variant choices and the
  * tuned classes (candidate times, choice) as text lines into buf. */
 #define SP_SPLIT_AUTO 127
