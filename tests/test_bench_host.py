@@ -49,3 +49,16 @@ def test_cpu_oracle_small_shape_matches_itself_and_decodes():
     resp, secs = orc.answer(cl.query(sh, 9))
     assert secs > 0 and (cl.decode(resp) == recs[9]).all()
     assert orc.db_mul_s(6, 2) > 0
+
+
+def test_integer_roofline_from_the_committed_counts():
+    """Items per batch and the issue-slot fractions that bench.py reports
+    next to each batch (profiles/int_pipe.json)."""
+    p, sh = P.PARAMS, P.SHAPE_1GIB
+    assert bench.expansion_outputs(p, sh.nu1, sh.nu2) == 1142
+    r = bench.int_roofline(p, sh, 32, {"fold": 7.11, "expand": 4.58}, 2070.0)
+    if r is None:
+        return
+    assert r["fold"]["items"] == {"k_fold_level<1>": 32 * 4 * 255, "k_acc_to_raw": 32 * 4 * 2 * 256}
+    for stage in ("fold", "expand"):
+        assert 0.2 < r[stage]["issue_frac"] < 1.2 and 0.1 < r[stage]["alu_pipe_frac"] < 1.2
