@@ -706,16 +706,16 @@ __device__ __forceinline__ uint32_t rescale_q(uint64_t x, int bits_out) {
     return (uint32_t)(neg ? ((0 - y) & mask) : y);
 }
 
-constexpr int PACK_MAX_N = 2;
-
 // Column col of query blockIdx.y: sum over r < n of
 // W_r * NTT(G^-1(ct[r*n+col].row0)) + e_{1+r} * NTT(ct[r*n+col].row1), then
 // raw, then row 0 rescaled to 2^q2_bits and rows 1..n to 4p.
 // The n*(t_conv + 1) transforms of a column (digit k < t_conv of ct r's row
 // 0, or its row 1 for k = t_conv) are spread over `split` CTAs; with
 // split > 1 each CTA publishes its partial sums and the last to arrive
-// finishes the column (no CTA waits for another).
-__global__ void __launch_bounds__(THREADS, 2) k_pack(const QDesc *__restrict__ qd, StageParams sp,
+// finishes the column (no CTA waits for another).  PACK_MAX_N (2 or 4) bounds
+// n: the n + 1 accumulators live in registers.
+template <int PACK_MAX_N>
+__global__ void __launch_bounds__(THREADS, PACK_MAX_N <= 2 ? 2 : 1) k_pack(const QDesc *__restrict__ qd, StageParams sp,
                                                  const TwiddleSet *__restrict__ tws, int split,
                                                  uint32_t *__restrict__ part, unsigned int *__restrict__ counters) {
     const QDesc &Q = qd[blockIdx.y];
@@ -809,7 +809,8 @@ __global__ void __launch_bounds__(THREADS, 2) k_pack(const QDesc *__restrict__ q
 
 cudaError_t launch_pack(const QDesc *qd, int nq, const StageParams &sp, const TwiddleSet *tw,
                         const SplitScratch *scr, cudaStream_t st, int split_shift) {
-    cudaError_t e = cudaFuncSetAttribute(k_pack, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    auto kernel = sp.n <= 2 ? k_pack<2> : k_pack<4>;
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     if (e != cudaSuccess) return e;
     // spread each column's n*(t_conv+1) transforms over CTAs while the launch
     // stays within the SMs and the scratch
@@ -822,7 +823,7 @@ cudaError_t launch_pack(const QDesc *qd, int nq, const StageParams &sp, const Tw
         while (split > 1 && (cols * split * (sp.n + 1) * 2 > (uint64_t)scr->slots * 4 || cols > (uint64_t)scr->counter_slots))
             split--;
     }
-    k_pack<<<dim3(sp.n * split, nq), THREADS, SMEM_BYTES, st>>>(qd, sp, tw, split, scr ? scr->part : nullptr,
+    kernel<<<dim3(sp.n * split, nq), THREADS, SMEM_BYTES, st>>>(qd, sp, tw, split, scr ? scr->part : nullptr,
                                                                scr ? scr->counters : nullptr);
     return cudaGetLastError();
 }

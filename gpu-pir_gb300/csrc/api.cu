@@ -298,7 +298,8 @@ int guard_self_test(sp_ctx *c) {
 
 int check_params(const sp_params *p) {
     if (!p) return fail(SP_ERR_INVALID, "params is NULL");
-    if (p->n < 1 || p->n > 2) return fail(SP_ERR_UNSUPPORTED, "n must be 1 or 2");
+    if (p->n != 1 && p->n != 2 && p->n != 4)
+        return fail(SP_ERR_UNSUPPORTED, "n must be 1, 2 or 4 (n*n plaintext polynomials per record, a power of two)");
     if (p->pt_bits < 1 || p->pt_bits > 8) return fail(SP_ERR_UNSUPPORTED, "pt_bits must be in [1, 8]");
     for (int t : {p->t_exp_left, p->t_exp_right, p->t_gsw, p->t_conv})
         if (t < 3 || t > 56) return fail(SP_ERR_UNSUPPORTED, "gadget lengths must be in [3, 56]");

@@ -47,7 +47,7 @@ typedef struct sp_ctx sp_ctx;
 /* Ring/gadget parameters shared by every database and client of a context.
  * Replaces the compile-time constants of gpu-pir/params.cuh:49-71. */
 typedef struct sp_params {
-    int32_t n;           /* plaintext matrices are n x n (1 or 2) */
+    int32_t n;           /* plaintext matrices are n x n (1, 2 or 4) */
     int32_t pt_bits;     /* plaintext modulus p = 2^pt_bits (<= 8) */
     int32_t t_exp_left;  /* expansion gadget length, first-dimension branch */
     int32_t t_exp_right; /* expansion gadget length, GSW-bit branch */

@@ -1,5 +1,5 @@
 """The answer path across parameter sets at the edges of the supported
-range (gadget lengths 3 and 56, 1- and 4-bit plaintexts, n = 1 and 2,
+range (gadget lengths 3 and 56, 1- and 4-bit plaintexts, n = 1, 2 and 4,
 q2_bits from pt_bits + 2 to 32), on small shapes: the GPU response equals
 the oracle's bit for bit.  Whether a record decodes depends on the noise
 budget of the set, so decoding is checked only for the sets that have one."""
@@ -23,6 +23,10 @@ SETS = [
      P.DbShape(5, 3), True),
     (P.SpiralParams(n=1, pt_bits=4, t_exp_left=8, t_exp_right=8, t_gsw=4, t_conv=4, q2_bits=28),
      P.DbShape(5, 3), True),
+    # n = 4: 16 plaintext polynomials per record, a 5 x 4 packed response;
+    # 128 combos per block at nu2 = 3, the tensor-core shape
+    (P.SpiralParams(n=4, pt_bits=8, t_exp_left=8, t_exp_right=8, t_gsw=7, t_conv=4, q2_bits=22),
+     P.DbShape(7, 3), True),
 ]
 
 
@@ -48,3 +52,13 @@ def test_param_set_matches_oracle(k):
         assert np.array_equal(b, r), f"set {k}: batched response differs"
         if decodes:
             assert np.array_equal(cl.decode(r), recs[i]), f"set {k}: record {i} does not decode"
+
+
+def test_unsupported_n_rejected():
+    """n*n must be a power of two (the combo blocks of the image): n = 3 and
+    n = 5 are refused when the context is created."""
+    from spiralpir.lib import SpiralError
+    for n in (3, 5):
+        with pytest.raises(SpiralError) as e:
+            SpiralGPU(P.SpiralParams(n=n))
+        assert e.value.code == 6
