@@ -350,6 +350,19 @@ def cpu_baseline(orc: CpuOracle, q, gpu_resp: np.ndarray) -> dict:
                       "beforehand (not timed)"}
 
 
+def init_ranks(timeout_s: float | None = None) -> None:
+    """The gloo process group of a multi-replica run (one rank per GPU),
+    with a bounded timeout: a rank that fails or exits before a collective
+    makes the others' next collective raise after `timeout_s` (default
+    $SPIRALPIR_PG_TIMEOUT_S or 600 s) instead of waiting forever."""
+    import datetime
+
+    import torch.distributed as dist
+    if timeout_s is None:
+        timeout_s = float(os.environ.get("SPIRALPIR_PG_TIMEOUT_S", "600"))
+    dist.init_process_group("gloo", timeout=datetime.timedelta(seconds=timeout_s))
+
+
 def max_over_ranks(values, world: int) -> list:
     """Element-wise maximum of per-rank figures over all ranks (one gloo
     all-reduce); the figures themselves when world == 1."""
@@ -414,7 +427,7 @@ def run_gpu(args, rank, world, local):
     barrier = None
     if world > 1:
         import torch.distributed as dist
-        dist.init_process_group("gloo")
+        init_ranks()
         barrier = dist.barrier
     # clocks are sampled from before the warm-up; samples inside the timed
     # regions (the staged run, the multiply alone, the end-to-end loop) count
@@ -506,6 +519,14 @@ def run_gpu(args, rank, world, local):
             entry["clocks"] = clocks.summary(clocks.windows[-2:])
             entry["roofline_int"] = int_roofline(p, sh, B, entry["stages_ms"],
                                                  (entry["clocks"] or clk or {}).get("sm_mhz"))
+            # what 8x the single-query rate would need of the per-query stages
+            sm = entry["stages_ms"]
+            per_q = (ms / batch) / 8
+            entry["gap_to_8x"] = {
+                "target_ms_per_query": per_q, "measured_ms_per_query": bms / B,
+                "expand_fold_ms_per_query": (sm["expand"] + sm["fold"]) / B,
+                "expand_fold_budget_ms_per_query": per_q - (sm["db_mul"] + sm["pack"] + sm["convert"]) / B,
+                "bound": "expansion and fold: length-2048 transforms at the issue fractions of roofline_int"}
             batched.append(entry)
         gpu2.close()
     other = None
