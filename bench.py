@@ -459,11 +459,14 @@ def run_gpu(args, rank, world, local):
     lat = []
     resp_bytes = int(gpu.response_bytes)
     out = np.empty(resp_bytes, dtype=np.uint8)
+    # host buffers in the C ABI's layout (uint64 CRT residues), as a caller
+    # of sp_answer holds them
+    q64 = [np.ascontiguousarray(q, dtype=np.uint64) for q in queries]
     with clocks.window():
         t_e2e = time.perf_counter()
         for i in range(args.steps):
             t1 = time.perf_counter()
-            gpu.answer(1, 1, queries[i % len(queries)], out=out)
+            gpu.answer(1, 1, q64[i % len(q64)], out=out)
             lat.append(time.perf_counter() - t1)
         e2e_s = time.perf_counter() - t_e2e
     clk = clocks.summary(clocks.windows)
