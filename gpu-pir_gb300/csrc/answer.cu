@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_expand_round(const QDesc *
             const int sh = bits * k;
             d[j] = (sh < 32 ? __funnelshift_r(x.x, x.y, sh) : x.y >> (sh - 32)) & (uint32_t)mask;
         }
-        ntt_fwd(d, twf, buf, c, t, bar);
+        ntt_fwd<1>(d, twf, buf, c, t, bar);   // digits below 2^19 (t >= 3)
         mac16(acc0, d, W + ((size_t)(0 * tk + k) * 2 + g) * D + VPT * t, c);
         mac16(acc1, d, W + ((size_t)(1 * tk + k) * 2 + g) * D + VPT * t, c);
     }
@@ -448,7 +448,7 @@ __global__ void __launch_bounds__(THREADS, 2) k_regev_to_gsw(const QDesc *__rest
         for (int k = 0; k < sp.t_conv; k++) {
             uint32_t d[VPT];
             digits(d, raw, bits * k, mask);
-            ntt_fwd(d, tw_fwd(x), x.buf, c, x.t, x.bar);
+            ntt_fwd<1>(d, tw_fwd(x), x.buf, c, x.t, x.bar);
             const int col = row + 2 * k;
             mac16(acc0, d, Q.conv + ((size_t)(0 * kc + col) * 2 + x.g) * D + VPT * x.t, c);
             mac16(acc1, d, Q.conv + ((size_t)(1 * kc + col) * 2 + x.g) * D + VPT * x.t, c);
@@ -580,7 +580,7 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_fold_level(const QDesc *__
                 d[j] = a >= b ? a - b : a + c.p - b;
             }
         }
-        ntt_fwd(d, twf, buf, c, t, bar);
+        ntt_fwd<2>(d, twf, buf, c, t, bar);   // digit differences below p
         const int col = row + 2 * k;
         mac16(acc0, d, C + ((size_t)(0 * gc + col) * 2 + g) * D + VPT * t, c);
         mac16(acc1, d, C + ((size_t)(1 * gc + col) * 2 + g) * D + VPT * t, c);
@@ -745,7 +745,7 @@ __global__ void __launch_bounds__(THREADS, PACK_MAX_N <= 2 ? 2 : 1) k_pack(const
             for (int j = 0; j < VPT; j++) raw[j] = ct[x.t + GROUP * j];
             uint32_t d[VPT];
             digits(d, raw, bits * k, mask);
-            ntt_fwd(d, tw_fwd(x), x.buf, c, x.t, x.bar);
+            ntt_fwd<1>(d, tw_fwd(x), x.buf, c, x.t, x.bar);
 #pragma unroll
             for (int a = 0; a <= PACK_MAX_N; a++)
                 if (a <= n) mac16(acc[a], d, W + ((size_t)(a * tcv + k) * 2 + x.g) * D + VPT * x.t, c);

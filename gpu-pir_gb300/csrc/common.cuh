@@ -13,7 +13,9 @@
 //   layout C: thread t holds e = 16*t + j         stages h = 4, 2, 1
 // Raw-domain work (digits, inverse CRT) uses layout A (coalesced), NTT-domain
 // work (key products) uses layout C (16 consecutive slots per thread).
-// Butterflies are Harvey's lazy butterflies with Shoup products (values < 4p
+// Digit transforms (inputs below 2^19 or p) skip the per-butterfly
+// reduction and reduce once or twice per transform (ntt_fwd<LAZY>).
+// Other butterflies are Harvey's lazy butterflies with Shoup products (values < 4p
 // forward, < 2p inverse); the transposes use an XOR swizzle that is
 // bank-conflict free for all three layouts.  Both directions read one
 // twiddle table per prime: the inverse twiddle of block i at the stage with
@@ -175,6 +177,15 @@ __device__ __forceinline__ void ct_bfly(uint32_t &x, uint32_t &y, uint2 w, uint3
     y = xr - t + 2 * p;
 }
 
+// Cooley-Tukey butterfly without reducing x: for x, y below B the outputs
+// are below B + 2p (the Shoup product is below 2p for any 32-bit y).
+__device__ __forceinline__ void ct_bfly_lazy(uint32_t &x, uint32_t &y, uint2 w, uint32_t p) {
+    const uint32_t t = shoup_mul(y, w.x, w.y, p);
+    const uint32_t xr = x;
+    x = xr + t;
+    y = xr - t + 2 * p;
+}
+
 // Gentleman-Sande butterfly with the twiddle -w: x + y and (x - y)(-w) =
 // (y - x) w, both in [0, 2p) for inputs below 2p.
 __device__ __forceinline__ void gs_bfly_neg(uint32_t &x, uint32_t &y, uint2 w, uint32_t p) {
@@ -189,9 +200,18 @@ __device__ __forceinline__ int baseA(int t) { return swz(t); }
 __device__ __forceinline__ int baseB(int t) { return swz(128 * (t >> 3) + (t & 7)); }
 __device__ __forceinline__ int baseC(int t) { return swz(16 * t); }
 
-// Forward NTT of one plane.  v: layout A in (values < 4p), layout C out
-// (values < 4p).  tw: forward table of this prime (shared memory).
-// buf: 2 x 2048 words of shared memory private to the group.
+// Forward NTT of one plane, layout A in, layout C out.  tw: forward table
+// of this prime (shared memory).  buf: 2 x 2048 words of shared memory
+// private to the group.  Value bounds (p < 2^28, 16p + 2^19 < 2^32 for
+// both primes; a stage adds less than 2p to the bound of a lazy butterfly):
+//   LAZY = 0  Harvey butterflies: in and out below 4p;
+//   LAZY = 1  digit inputs below 2^19: lazy butterflies, one min(x, x - 8p)
+//             before phase C; out below 2^19 + 14p;
+//   LAZY = 2  inputs below 8p: as 1 with one more min(x, x - 8p) before
+//             phase B; out below 14p.
+// Lazy outputs are meant for Montgomery products, which take any 32-bit
+// operand.
+template <int LAZY = 0>
 __device__ __forceinline__ void ntt_fwd(uint32_t (&v)[VPT], const uint2 *__restrict__ tw,
                                         uint32_t *buf, const Prime &c, int t, int bar_id) {
     const uint32_t p = c.p;
@@ -201,7 +221,14 @@ __device__ __forceinline__ void ntt_fwd(uint32_t (&v)[VPT], const uint2 *__restr
         const int dj = 8 >> L;
 #pragma unroll
         for (int j = 0; j < VPT; j++)
-            if ((j & dj) == 0) ct_bfly(v[j], v[j + dj], tw[(1 << L) + j / (2 * dj)], p);
+            if ((j & dj) == 0) {
+                if constexpr (LAZY) ct_bfly_lazy(v[j], v[j + dj], tw[(1 << L) + j / (2 * dj)], p);
+                else ct_bfly(v[j], v[j + dj], tw[(1 << L) + j / (2 * dj)], p);
+            }
+    }
+    if constexpr (LAZY == 2) {
+#pragma unroll
+        for (int j = 0; j < VPT; j++) v[j] = min(v[j], v[j] - 8 * p);
     }
     // transpose A -> B
     {
@@ -222,9 +249,16 @@ __device__ __forceinline__ void ntt_fwd(uint32_t (&v)[VPT], const uint2 *__restr
             const int dj = 8 >> (L - 4);
 #pragma unroll
             for (int j = 0; j < VPT; j++)
-                if ((j & dj) == 0)
-                    ct_bfly(v[j], v[j + dj], tw[(1 << L) + (bb << (L - 4)) + (j >> (8 - L))], p);
+                if ((j & dj) == 0) {
+                    const uint2 w = tw[(1 << L) + (bb << (L - 4)) + (j >> (8 - L))];
+                    if constexpr (LAZY) ct_bfly_lazy(v[j], v[j + dj], w, p);
+                    else ct_bfly(v[j], v[j + dj], w, p);
+                }
         }
+    }
+    if constexpr (LAZY) {
+#pragma unroll
+        for (int j = 0; j < VPT; j++) v[j] = min(v[j], v[j] - 8 * p);
     }
     // transpose B -> C
     {
@@ -243,7 +277,10 @@ __device__ __forceinline__ void ntt_fwd(uint32_t (&v)[VPT], const uint2 *__restr
         const int dj = 4 >> (L - 8);
 #pragma unroll
         for (int j = 0; j < VPT; j++)
-            if ((j & dj) == 0) ct_bfly(v[j], v[j + dj], tw[(1 << L) + (j / (2 * dj)) * GROUP + t], p);
+            if ((j & dj) == 0) {
+                if constexpr (LAZY) ct_bfly_lazy(v[j], v[j + dj], tw[(1 << L) + (j / (2 * dj)) * GROUP + t], p);
+                else ct_bfly(v[j], v[j + dj], tw[(1 << L) + (j / (2 * dj)) * GROUP + t], p);
+            }
     }
 }
 
