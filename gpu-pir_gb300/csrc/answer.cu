@@ -321,6 +321,145 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_expand_round(const QDesc *
     }
 }
 
+// Round r with many outputs: CTA blockIdx.x = parent p < 2^r of query
+// blockIdx.y computes both children, p and p + 2^r (k_expand_round's
+// outputs of those indices, the same residues).  With k = 2^r and
+// tau = D / k + 1, tau(x^-k c) = -x^-k tau(c) (k * tau = D + k, x^D = -1),
+// so the upper child's raw(tau(.).row0) is the lower's rotated by k with a
+// sign change: one inverse transform and one gather per parent instead of
+// two.  The children share the key (left for even indices, right for odd,
+// and p + 2^r has p's parity for r >= 1; right for both at r = 0).
+__global__ void __launch_bounds__(THREADS, 2) k_expand_pair(const QDesc *__restrict__ qd, int r, StageParams sp,
+                                                           const TwiddleSet *__restrict__ tws,
+                                                           const uint32_t *__restrict__ neg1) {
+    const QDesc &Q = qd[blockIdx.y];
+    const int pr = blockIdx.x, half = 1 << r;
+    if (!Q.active || r >= Q.g || pr >= half) return;
+    const int max_bits = sp.t_gsw * Q.nu2;
+    auto live = [&](int i) {
+        if (Q.stop > 0 && r > Q.stop && (i & 1)) return false;
+        if (Q.stop > 0 && r == Q.stop && (i & 1) && (i / 2) >= max_bits) return false;
+        return true;
+    };
+    const bool live_lo = live(pr), live_up = live(pr + half);
+    if (!live_lo && !live_up) return;
+    extern __shared__ __align__(16) uint32_t smem[];
+    pdl_launch_dependents();
+    load_twiddles(smem, tws);   // constant: may overlap the previous round
+    pdl_wait();
+    const int g = threadIdx.x >> 7, t = threadIdx.x & (GROUP - 1), bar = 1 + g;
+    const Prime c = prime_of(g);
+    uint32_t *bufs = smem + TW_WORDS;
+    uint32_t *buf = bufs + g * 2 * D;
+    const uint2 *twf = tw_of(smem, g), *twi = twf;
+    __syncthreads();
+    const uint32_t *ct = r == 0 ? Q.query : Q.v[r & 1] + (size_t)pr * 4 * D;
+    const uint32_t *n1 = neg1 + ((size_t)r * 2 + g) * D;
+    const uint32_t tau = (uint32_t)(D >> r) + 1;
+    {
+        // raw(tau(c.row0)) of the parent: INTT per prime, inverse CRT by all
+        const uint32_t *row0 = ct + g * D;
+        uint32_t v[VPT];
+#pragma unroll
+        for (int j = 0; j < VPT; j++) v[j] = row0[auto_slot(VPT * t + j, tau)];
+        ntt_inv(v, twi, buf, c, t, bar);
+#pragma unroll
+        for (int j = 0; j < VPT; j++) buf[t + GROUP * j] = v[j];
+    }
+    __syncthreads();
+    uint64_t *raws = reinterpret_cast<uint64_t *>(bufs + 2 * 2 * D);
+#pragma unroll
+    for (int j = 0; j < VPT; j++) {
+        if ((j * 2) / VPT != g) continue;
+        const int e = t + GROUP * j;
+        raws[e] = icrt(bufs[e], bufs[2 * D + e]);
+    }
+    __syncthreads();
+    const bool left = (r != 0) && !(pr & 1);
+    const int tk = left ? sp.t_left : sp.t_right;
+    const uint32_t *W = (left ? Q.left : Q.right) + (size_t)r * 2 * tk * 2 * D;
+    const int bits = bits_per(tk);
+    const uint32_t m32 = (uint32_t)((1ull << bits) - 1);
+    const int zb = VPT * t;
+#pragma unroll 1
+    for (int h = 0; h < 2; h++) {
+        const int i = pr + h * half;
+        const bool upper = h == 1;
+        if (upper) {
+            // raws <- -x^-k raws: position e takes -raws[e + k] below D - k,
+            // raws[e + k - D] from there on (canonical mod q)
+            uint64_t w[D / THREADS];
+#pragma unroll
+            for (int u = 0; u < D / THREADS; u++) {
+                const int e = threadIdx.x + THREADS * u, src = e + half;
+                if (src < D) {
+                    const uint64_t a = raws[src];
+                    w[u] = a ? QQ - a : 0;
+                } else {
+                    w[u] = raws[src - D];
+                }
+            }
+            __syncthreads();   // every read of raws (and of the lower child's staging) done
+#pragma unroll
+            for (int u = 0; u < D / THREADS; u++) raws[threadIdx.x + THREADS * u] = w[u];
+            __syncthreads();
+        }
+        if (!(upper ? live_up : live_lo)) continue;
+        uint32_t acc0[VPT], acc1[VPT];
+#pragma unroll
+        for (int j = 0; j < VPT; j++) acc0[j] = acc1[j] = 0;
+#pragma unroll 1
+        for (int k = 0; k < tk; k++) {
+            uint32_t d[VPT];
+            const int sh = bits * k;
+#pragma unroll
+            for (int j = 0; j < VPT; j++) {
+                const uint2 x = reinterpret_cast<const uint2 *>(raws)[t + GROUP * j];
+                d[j] = (sh < 32 ? __funnelshift_r(x.x, x.y, sh) : x.y >> (sh - 32)) & m32;
+            }
+            ntt_fwd<1>(d, twf, buf, c, t, bar);   // digits below 2^19 (t >= 3)
+            mac16(acc0, d, W + ((size_t)(0 * tk + k) * 2 + g) * D + VPT * t, c);
+            mac16(acc1, d, W + ((size_t)(1 * tk + k) * 2 + g) * D + VPT * t, c);
+        }
+        // output rows: row 0 = v.row0 + acc0, row 1 = v.row1 + acc1 + tau(v.row1),
+        // v = c (lower child) or x^-k c (upper)
+        const bool to_sel = r == Q.g - 1 && !(i & 1) && (i / 2) < (1 << Q.nu1);
+        if (to_sel) __syncthreads();   // every group is done with its transpose buffers
+        for (int row = 0; row <= 1; row++) {
+            const uint32_t *src = ct + (row * 2 + g) * D;
+            uint32_t o[VPT];
+            ld16(o, src + zb);
+            if (upper) {
+                uint32_t nn[VPT];
+                ld16(nn, n1 + zb);
+#pragma unroll
+                for (int j = 0; j < VPT; j++) o[j] = reduce2(mont_mul(o[j], nn[j], c.p, c.pinv), c.p);
+            }
+#pragma unroll
+            for (int j = 0; j < VPT; j++) o[j] = canon4(o[j] + (row == 0 ? acc0[j] : acc1[j]), c.p);
+            if (row == 1) {
+#pragma unroll
+                for (int j = 0; j < VPT; j++) {
+                    const int zs = auto_slot(zb + j, tau);
+                    uint32_t tb = src[zs];
+                    if (upper) tb = reduce2(mont_mul(tb, n1[zs], c.p, c.pinv), c.p);
+                    o[j] = canon4(o[j] + tb, c.p);
+                }
+            }
+            if (r + 1 < Q.g) st16(Q.v[(r + 1) & 1] + (size_t)i * 4 * D + (row * 2 + g) * D + zb, o);
+            if (r == Q.capture && (i & 1) && (i / 2) < max_bits)
+                st16(Q.gsw_in + (size_t)(i / 2) * 4 * D + (row * 2 + g) * D + zb, o);
+            if (to_sel) st16(bufs + (row * 2 + g) * D + zb, o);
+        }
+        if (to_sel) {
+            __syncthreads();
+            uint4 *sl = reinterpret_cast<uint4 *>(Q.sel + (size_t)(i / 2) * D * 4);
+            for (int z = threadIdx.x; z < D; z += blockDim.x)
+                sl[z] = make_uint4(bufs[z], bufs[D + z], bufs[2 * D + z], bufs[3 * D + z]);
+        }
+    }
+}
+
 cudaError_t launch_expand_round(const QDesc *qd, int nq, int r, int max_out, const StageParams &sp,
                                 const TwiddleSet *tw, const uint32_t *neg1, const SplitScratch *scr,
                                 cudaStream_t st, int split_shift) {
@@ -345,10 +484,22 @@ cudaError_t launch_expand_round(const QDesc *qd, int nq, int r, int max_out, con
         if (e != cudaSuccess) return e;
     } else {
         const int smem = SMEM_BYTES + D * 8;
-        cudaError_t e = cudaFuncSetAttribute(k_expand_round<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-        if (e != cudaSuccess) return e;
-        e = launch_ex(k_expand_round<1>, dim3(max_out, nq), dim3(THREADS), smem, st, r > 0, qd, r, sp, tw, neg1, 1,
-                      (uint32_t *)nullptr, (unsigned int *)nullptr);
+        const uint64_t pairs = (uint64_t)std::max(1, max_out / 2) * nq;
+        cudaError_t e;
+        if (pairs >= 4ull * sms) {
+            // at least two waves of parents: one CTA per parent computes both
+            // children (one inverse transform instead of two)
+            e = cudaFuncSetAttribute(k_expand_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e != cudaSuccess) return e;
+            e = launch_ex(k_expand_pair, dim3(std::max(1, max_out / 2), nq), dim3(THREADS), smem, st, r > 0, qd, r, sp,
+                          tw, neg1);
+        } else {
+            // fewer: one CTA per output keeps every slot busy
+            e = cudaFuncSetAttribute(k_expand_round<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e != cudaSuccess) return e;
+            e = launch_ex(k_expand_round<1>, dim3(max_out, nq), dim3(THREADS), smem, st, r > 0, qd, r, sp, tw, neg1,
+                          1, (uint32_t *)nullptr, (unsigned int *)nullptr);
+        }
         if (e != cudaSuccess) return e;
     }
     return cudaGetLastError();
