@@ -5,6 +5,8 @@
 // modulo prime g.  Raw (56-bit) values are rebuilt by an inverse CRT of both
 // groups' INTT outputs exchanged through shared memory.
 #include <algorithm>
+#include <cstdlib>
+#include <string>
 #include <utility>
 
 #include "answer.cuh"
@@ -460,12 +462,28 @@ __global__ void __launch_bounds__(THREADS, 2) k_expand_pair(const QDesc *__restr
     }
 }
 
+namespace {
+// Expansion kernel of every round: chosen by size (launch_expand_round), or
+// forced for all rounds by SPIRALPIR_EXPAND_KERNEL = split | single | pair,
+// read once per process (the tests answer the same queries with each).
+int expand_kernel_override() {
+    static const int v = [] {
+        const char *e = std::getenv("SPIRALPIR_EXPAND_KERNEL");
+        if (!e) return 0;
+        const std::string s(e);
+        return s == "split" ? 1 : s == "single" ? 2 : s == "pair" ? 3 : 0;
+    }();
+    return v;
+}
+}  // namespace
+
 cudaError_t launch_expand_round(const QDesc *qd, int nq, int r, int max_out, const StageParams &sp,
                                 const TwiddleSet *tw, const uint32_t *neg1, const SplitScratch *scr,
                                 cudaStream_t st, int split_shift) {
     const uint64_t total = (uint64_t)max_out * nq;
     const int sms = sm_count();
-    if (total < 2ull * sms) {
+    const int force = expand_kernel_override();
+    if (force ? force == 1 : total < 2ull * sms) {
         // few outputs: 2 groups per prime split the digits; with scratch,
         // each output also spreads over `split` CTAs while that stays within
         // one CTA per SM, at least one digit transform per group
@@ -486,7 +504,7 @@ cudaError_t launch_expand_round(const QDesc *qd, int nq, int r, int max_out, con
         const int smem = SMEM_BYTES + D * 8;
         const uint64_t pairs = (uint64_t)std::max(1, max_out / 2) * nq;
         cudaError_t e;
-        if (pairs >= 4ull * sms) {
+        if (force ? force == 3 : pairs >= 4ull * sms) {
             // at least two waves of parents: one CTA per parent computes both
             // children (one inverse transform instead of two)
             e = cudaFuncSetAttribute(k_expand_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
