@@ -146,6 +146,42 @@ __global__ void k_widen(const uint32_t *__restrict__ in, uint64_t *__restrict__ 
     }
 }
 
+// Inputs of an answer run read straight from the lane's pinned staging (host
+// memory the device addresses directly): block k copies descriptor k to the
+// device and narrows query k (u64 [2 rows][2 primes][D]) into its slot's
+// u32 planes, as k_narrow does.
+// Block (b, k) of STAGE_BLOCKS per query: a thread issues its STAGE_VPT host
+// loads together, then narrows them.
+constexpr int STAGE_THREADS = 256, STAGE_VPT = 4, STAGE_BLOCKS = 4 * D / (STAGE_THREADS * STAGE_VPT);
+__global__ void __launch_bounds__(STAGE_THREADS) k_stage_in(const QDesc *__restrict__ h_qd, QDesc *__restrict__ d_qd,
+                                                            const uint64_t *__restrict__ h_query) {
+    const int k = blockIdx.y;
+    if (blockIdx.x == 0) {
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(h_qd + k);
+        uint32_t *dst = reinterpret_cast<uint32_t *>(d_qd + k);
+        for (int w = threadIdx.x; w < (int)(sizeof(QDesc) / 4); w += blockDim.x) dst[w] = src[w];
+    }
+    uint32_t *q = const_cast<uint32_t *>(h_qd[k].query);
+    const uint64_t *in = h_query + (size_t)k * 4 * D;
+    const int i0 = blockIdx.x * STAGE_THREADS * STAGE_VPT + threadIdx.x;
+    uint64_t v[STAGE_VPT];
+#pragma unroll
+    for (int u = 0; u < STAGE_VPT; u++) v[u] = in[i0 + u * STAGE_THREADS];
+#pragma unroll
+    for (int u = 0; u < STAGE_VPT; u++) {
+        const int i = i0 + u * STAGE_THREADS;
+        const Prime c = prime_of((i / D) & 1);
+        q[i] = mod_u64(((uint64_t)((uint32_t)(v[u] >> 32) % c.p) << 32) | (uint32_t)v[u], c);
+    }
+}
+
+cudaError_t launch_stage_in(const QDesc *h_qd, QDesc *d_qd, const uint64_t *h_query, int nq, cudaStream_t st) {
+    static_assert(sizeof(QDesc) % 4 == 0, "descriptor words");
+    static_assert(STAGE_BLOCKS * STAGE_THREADS * STAGE_VPT == 4 * D, "query tiling");
+    k_stage_in<<<dim3(STAGE_BLOCKS, nq), STAGE_THREADS, 0, st>>>(h_qd, d_qd, h_query);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_narrow(const uint64_t *in, uint32_t *out, uint64_t planes, bool to_mont, cudaStream_t st) {
     const uint64_t total = planes * D;
     int blocks = (int)((total + 255) / 256);
@@ -1004,7 +1040,10 @@ uint64_t response_bytes(const StageParams &sp) {
 
 // Serialise: first n*D values of q2_bits, then n*n*D values of pt_bits+2,
 // least significant bit first, packed into little-endian 32-bit words.
-__global__ void k_bitpack(const QDesc *__restrict__ qd, StageParams sp, uint64_t words) {
+__global__ void k_bitpack(const QDesc *__restrict__ qd, StageParams sp, uint64_t words, const int *__restrict__ d_err,
+                          int *__restrict__ h_err) {
+    // every earlier kernel of the run has completed: pass on its error flag
+    if (h_err && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *h_err = *d_err;
     const QDesc &Q = qd[blockIdx.y];
     if (!Q.active) return;
     const uint64_t n0 = (uint64_t)sp.n * D;
@@ -1036,10 +1075,11 @@ __global__ void k_bitpack(const QDesc *__restrict__ qd, StageParams sp, uint64_t
     }
 }
 
-cudaError_t launch_bitpack(const QDesc *qd, int nq, const StageParams &sp, uint64_t resp_bytes, cudaStream_t st) {
+cudaError_t launch_bitpack(const QDesc *qd, int nq, const StageParams &sp, uint64_t resp_bytes, cudaStream_t st,
+                           const int *d_err, int *h_err) {
     const uint64_t words = resp_bytes / 4;
     int blocks = (int)((words + 255) / 256);
-    k_bitpack<<<dim3(blocks, nq), 256, 0, st>>>(qd, sp, words);
+    k_bitpack<<<dim3(blocks, nq), 256, 0, st>>>(qd, sp, words, d_err, h_err);
     return cudaGetLastError();
 }
 

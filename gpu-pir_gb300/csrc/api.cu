@@ -650,14 +650,8 @@ int choose_mul_variant(sp_ctx *c, Lane &L, int db_id, const Db &db, const QDesc 
 // Uploads of an answer's inputs: the queries from the lane's pinned staging,
 // converted to u32 residues, and the descriptors from L.h_qd.
 cudaError_t enqueue_inputs(Lane &L, int nq, cudaStream_t st) {
-    cudaError_t e = cudaSuccess;
-    for (int k = 0; k < nq && !e; k++) {
-        e = cudaMemcpyAsync(L.slots[k].query64, L.h_query + (uint64_t)k * 4 * D, 4ull * D * 8,
-                            cudaMemcpyHostToDevice, st);
-        if (!e) e = launch_narrow(L.slots[k].query64, L.slots[k].query32, 4, false, st);   // 2 rows x 2 primes
-    }
-    if (!e) e = cudaMemcpyAsync(L.d_qd, L.h_qd, sizeof(QDesc) * nq, cudaMemcpyHostToDevice, st);
-    return e;
+    // one kernel reads the descriptors and queries from the pinned staging
+    return launch_stage_in(L.h_qd, L.d_qd, L.h_query, nq, st);
 }
 
 // Autotuner of the narrow launches' split schedule (answer.cuh
@@ -702,9 +696,11 @@ int tune_split(sp_ctx *c, Lane &L, const std::vector<int64_t> &key, Enqueue &enq
 
 // Run the answer pipeline for queries in slots [0, nq) (descriptors in
 // L.h_qd).  Without `io` the queries and descriptors are already on the
-// device (sp_stage_query); with `io` the pipeline itself uploads them from the
-// lane's pinned staging (L.h_query, L.h_qd) and downloads the responses to
-// L.h_resp and the error flag to L.h_err, all inside the captured graph.
+// device (sp_stage_query); with `io` the pipeline's first kernel reads them
+// from the lane's pinned staging (L.h_query, L.h_qd: host memory the device
+// addresses directly) and its last writes the responses to L.h_resp (the
+// descriptors point there) and the error flag to L.h_err: no copies in the
+// captured graph.
 // Records stage events.
 //
 // The launches depend only on the batch plan: query count, the largest
@@ -789,14 +785,11 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
             e = launch_fold_level(L.d_qd, nq, lvl, sp.T << (max_nu2 - 1 - lvl), sp, c->d_tw, &L.split, st, cur_shift);
         if (!e) e = cudaEventRecordWithFlags(L.ev[4], st, ev_flags);
         if (!e) e = launch_pack(L.d_qd, nq, sp, c->d_tw, &L.split, st, cur_shift);
-        if (!e) e = launch_bitpack(L.d_qd, nq, sp, response_bytes(sp), st);
+        // with host I/O the responses (descriptors point into the pinned
+        // staging) and the error flag go to host memory from the kernel
+        if (!e) e = launch_bitpack(L.d_qd, nq, sp, response_bytes(sp), st, io ? L.d_err : nullptr,
+                                   io ? L.h_err : nullptr);
         if (!e) e = cudaEventRecordWithFlags(L.ev[5], st, ev_flags);
-        if (io) {
-            const uint64_t rb = response_bytes(sp);
-            for (int k = 0; k < nq && !e; k++)
-                e = cudaMemcpyAsync(L.h_resp + k * rb, L.slots[k].q.resp, rb, cudaMemcpyDeviceToHost, st);
-            if (!e) e = cudaMemcpyAsync(L.h_err, L.d_err, sizeof(int), cudaMemcpyDeviceToHost, st);
-        }
         return e;
     };
     // split schedule: forced, tuned earlier for this batch class, or tuned
@@ -844,7 +837,7 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
     } else {
         CU(enqueue(false));
     }
-    uint64_t launches = (uint64_t)max_g + 1 + 1 + (uint64_t)max_nu2 + 2 + (io ? (uint64_t)nq : 0);
+    uint64_t launches = (uint64_t)max_g + 1 + 1 + (uint64_t)max_nu2 + 2 + (io ? 1 : 0);
     for (const Group &gr : groups) {
         c->stats.db_mul_by_variant[gr.variant - 1]++;
         launches += gr.variant == 3 ? 3 * (uint64_t)((gr.count + TC_MAX_Q - 1) / TC_MAX_Q) : 1;
@@ -1435,6 +1428,8 @@ static int prepare(sp_ctx *c, Lane &L, int n, sp_request *reqs, std::vector<int>
         sl.client = r.client_id;
         sl.db = r.db_id;
         L.h_qd[k] = sl.q;
+        // the run writes this query's response straight into the pinned staging
+        L.h_qd[k].resp = L.h_resp + (uint64_t)k * response_bytes(c->sp);
         db_of_slot[k] = r.db_id;
         // into the lane's pinned staging; the pipeline uploads it
         memcpy(L.h_query + (uint64_t)k * 4 * D, r.query, 4ull * D * 8);
