@@ -220,19 +220,39 @@ def measured_traffic(algo_bytes: float):
     return float(d["traffic_over_algorithmic"]) * algo_bytes
 
 
-def expansion_outputs(p, nu1: int, nu2: int) -> int:
-    """Expansion outputs computed per query (every round's live outputs
-    after the reference's pruning, gpu-pir/expansion.cuh:92-97)."""
+def expansion_round_outputs(p, nu1: int, nu2: int) -> list:
+    """Live outputs of every expansion round of one query, after the
+    reference's pruning (gpu-pir/expansion.cuh:92-97)."""
     g, stop, max_bits = p.g(nu1, nu2), p.stop_round(nu2), p.t_gsw * nu2
-    n = 0
+    out = []
     for r in range(g):
+        n = 0
         for i in range(2 << r):
             if r > stop and i & 1:
                 continue
             if r == stop and i & 1 and i // 2 >= max_bits:
                 continue
             n += 1
-    return n
+        out.append(n)
+    return out
+
+
+def expansion_outputs(p, nu1: int, nu2: int) -> int:
+    """Expansion outputs computed per query."""
+    return sum(expansion_round_outputs(p, nu1, nu2))
+
+
+def expansion_kernel_outputs(p, nu1: int, nu2: int, B: int, sms: int = 152) -> dict:
+    """Outputs of a B-query batch by the expansion kernel that computes them
+    (the library's rule: a round with at least 2 x SMs outputs runs one CTA
+    per output, or one per parent with at least 4 x SMs parents; fewer
+    outputs run the split kernel, counted here with the one-per-output
+    figure)."""
+    out = {"k_expand_round<1>": 0, "k_expand_pair": 0}
+    for r, n in enumerate(expansion_round_outputs(p, nu1, nu2)):
+        paired = (2 << r) * B >= 2 * sms and (1 << r) * B >= 4 * sms
+        out["k_expand_pair" if paired else "k_expand_round<1>"] += n * B
+    return out
 
 
 def int_roofline(p, sh, B: int, stages_ms: dict, sm_mhz: float | None) -> dict | None:
@@ -252,10 +272,12 @@ def int_roofline(p, sh, B: int, stages_ms: dict, sm_mhz: float | None) -> dict |
     issue_peak = sms * 4 * sm_mhz * 1e6
     folds = B * p.T * ((1 << sh.nu2) - 1)
     polys = B * p.T * 2 * (1 << sh.nu2)
-    outs = B * expansion_outputs(p, sh.nu1, sh.nu2)
+    outs = expansion_kernel_outputs(p, sh.nu1, sh.nu2, B, sms)
+    if "k_expand_pair" not in k:     # counts captured before the paired kernel
+        outs = {"k_expand_round<1>": sum(outs.values())}
     out = {"sm_mhz": sm_mhz, "issue_peak_warp_inst_per_s": issue_peak, "source": "profiles/int_pipe.json"}
     for stage, parts, ms in (("fold", (("k_fold_level<1>", folds), ("k_acc_to_raw", polys)), stages_ms["fold"]),
-                             ("expand", (("k_expand_round<1>", outs),), stages_ms["expand"])):
+                             ("expand", tuple((name, n) for name, n in outs.items() if n), stages_ms["expand"])):
         inst = sum(k[name]["warp_inst_per_item"] * n for name, n in parts)
         alu = sum(k[name]["alu_inst_per_item"] * n for name, n in parts)
         alu_rate = k[parts[0][0]].get("alu_warp_inst_per_scheduler_cycle_peak") or 0.5
