@@ -1952,10 +1952,11 @@ int set_last_error(int code, const char *msg) { return fail(code, msg); }
 // Continuous batching: sp_submit queues a request (the query is copied); a
 // worker thread launches the queued requests, up to max_batch at a time, on
 // whichever lane is free, so a batch admitted while others run overlaps
-// with them on the GPU.  Lanes own their slots (device workspace sized under
-// the HBM budget), their stream and pinned response staging; a finished
-// lane's responses are copied to the callers' buffers and their tickets
-// completed.
+// with them on the GPU.  When more requests wait than a batch holds, a
+// batch gathers the oldest request's database's requests.  Lanes own their
+// slots (device workspace sized under the HBM budget), their stream and
+// pinned response staging; a finished lane's responses are copied to the
+// callers' buffers and their tickets completed.
 namespace {
 
 void complete(sp_ctx *c, uint64_t ticket, int status) {
@@ -1987,9 +1988,20 @@ void finish_lane(sp_ctx *c, Lane &L) {
 void launch_lane(sp_ctx *c, Lane &L) {
     TraceRange trace_("serve_batch");
     std::vector<Pending> batch;
-    while (!c->queue.empty() && (int)batch.size() < L.cap) {
-        Pending p = std::move(c->queue.front());
-        c->queue.pop_front();
+    // A queue that fits in one batch runs whole, in arrival order.  A longer
+    // one runs by database: the oldest request's database first, with its
+    // other queued requests (up to the lane's capacity, in arrival order),
+    // so that one pass over a database image serves as many queries as are
+    // waiting for it; requests for other databases keep their place.
+    const bool by_db = (int)c->queue.size() > L.cap;
+    const int db_first = c->queue.empty() ? 0 : c->queue.front().db_id;
+    for (auto qi = c->queue.begin(); qi != c->queue.end() && (int)batch.size() < L.cap;) {
+        if (by_db && qi->db_id != db_first) {
+            ++qi;
+            continue;
+        }
+        Pending p = std::move(*qi);
+        qi = c->queue.erase(qi);
         // requests that cannot run complete at once with their error
         auto ci = c->clients.find(p.client_id);
         auto di = c->dbs.find(p.db_id);
