@@ -60,5 +60,20 @@ def test_integer_roofline_from_the_committed_counts():
     if r is None:
         return
     assert r["fold"]["items"] == {"k_fold_level<1>": 32 * 4 * 255, "k_acc_to_raw": 32 * 4 * 2 * 256}
+    assert sum(r["expand"]["items"].values()) == 32 * 1142
     for stage in ("fold", "expand"):
         assert 0.2 < r[stage]["issue_frac"] < 1.2 and 0.1 < r[stage]["alu_pipe_frac"] < 1.2
+
+
+def test_expansion_outputs_by_kernel():
+    """The library's kernel choice per round, as the bench counts it: one
+    query runs no round on the paired kernel (its widest rounds have fewer
+    than 4 x SMs parents); 32 queries run rounds 5-9 on it."""
+    p, sh = P.PARAMS, P.SHAPE_1GIB
+    per_round = bench.expansion_round_outputs(p, sh.nu1, sh.nu2)
+    assert sum(per_round) == 1142 and len(per_round) == p.g(sh.nu1, sh.nu2)
+    one = bench.expansion_kernel_outputs(p, sh.nu1, sh.nu2, 1)
+    assert one == {"k_expand_round<1>": 1142, "k_expand_pair": 0}
+    b32 = bench.expansion_kernel_outputs(p, sh.nu1, sh.nu2, 32)
+    assert b32["k_expand_pair"] == 32 * sum(per_round[5:])
+    assert b32["k_expand_round<1>"] == 32 * sum(per_round[:5])
