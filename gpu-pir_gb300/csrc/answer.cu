@@ -201,6 +201,54 @@ cudaError_t launch_widen(const uint32_t *in, uint64_t *out, uint64_t planes, boo
 }
 
 // -------------------------------------------------------------- expansion
+// Output i of round r (rows first..last of this group's prime g):
+//   row 0 = v.row0 + acc0, row 1 = v.row1 + acc1 + tau(v.row1),
+// v = ct (the parent) or, for an upper output, x^-(2^r) ct (n1 in NTT form).
+// Written to the next round's buffer, to the GSW-bit inputs at the capture
+// round and, for the last round's even outputs, staged in `bufs` and written
+// as the first-dimension selector (one 16-byte slot [row 0 q1, row 0 q2,
+// row 1 q1, row 1 q2] per coefficient).  Every thread of the CTA calls it.
+__device__ __forceinline__ void expand_store(const QDesc &Q, int r, int i, bool upper, const uint32_t *ct,
+                                             const uint32_t *n1, uint32_t tau, int max_bits, int first, int last,
+                                             int g, int t, const Prime &c, uint32_t *bufs,
+                                             const uint32_t (&acc0)[VPT], const uint32_t (&acc1)[VPT]) {
+    const int zb = VPT * t;
+    const bool to_sel = r == Q.g - 1 && !(i & 1) && (i / 2) < (1 << Q.nu1);
+    if (to_sel) __syncthreads();   // every group is done with its transpose buffers
+    for (int row = first; row <= last; row++) {
+        const uint32_t *src = ct + (row * 2 + g) * D;
+        uint32_t o[VPT];
+        ld16(o, src + zb);
+        if (upper) {
+            uint32_t nn[VPT];
+            ld16(nn, n1 + zb);
+#pragma unroll
+            for (int j = 0; j < VPT; j++) o[j] = reduce2(mont_mul(o[j], nn[j], c.p, c.pinv), c.p);
+        }
+#pragma unroll
+        for (int j = 0; j < VPT; j++) o[j] = canon4(o[j] + (row == 0 ? acc0[j] : acc1[j]), c.p);
+        if (row == 1) {
+#pragma unroll
+            for (int j = 0; j < VPT; j++) {
+                const int zs = auto_slot(zb + j, tau);
+                uint32_t tb = src[zs];
+                if (upper) tb = reduce2(mont_mul(tb, n1[zs], c.p, c.pinv), c.p);
+                o[j] = canon4(o[j] + tb, c.p);
+            }
+        }
+        if (r + 1 < Q.g) st16(Q.v[(r + 1) & 1] + (size_t)i * 4 * D + (row * 2 + g) * D + zb, o);
+        if (r == Q.capture && (i & 1) && (i / 2) < max_bits)
+            st16(Q.gsw_in + (size_t)(i / 2) * 4 * D + (row * 2 + g) * D + zb, o);
+        if (to_sel) st16(bufs + (row * 2 + g) * D + zb, o);
+    }
+    if (to_sel) {
+        __syncthreads();
+        uint4 *sl = reinterpret_cast<uint4 *>(Q.sel + (size_t)(i / 2) * D * 4);
+        for (int z = threadIdx.x; z < D; z += blockDim.x)
+            sl[z] = make_uint4(bufs[z], bufs[D + z], bufs[2 * D + z], bufs[3 * D + z]);
+    }
+}
+
 // Round r for output index i = blockIdx.x of query blockIdx.y
 // (gpu-pir/expansion.cuh:87-166 semantics): the input is v[i] for i < 2^r
 // and x^(-2^r) * v[i - 2^r] above; the output is
@@ -317,46 +365,9 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_expand_round(const QDesc *
             if (threadIdx.x == 0) counters[(size_t)blockIdx.y * items + i] = 0;   // ready for the next launch
         }
     }
-    // output rows: row 0 = v.row0 + acc0, row 1 = v.row1 + acc1 + tau(v.row1)
-    const int zb = VPT * t;
-    const int first = GP == 2 ? sub : 0, last = GP == 2 ? sub : 1;
-    // first-dimension selectors (last round, even outputs): the four planes
-    // (row, prime) are staged in shared memory and written as one 16-byte
-    // slot [row 0 q1, row 0 q2, row 1 q1, row 1 q2] per coefficient
-    const bool to_sel = r == Q.g - 1 && !(i & 1) && (i / 2) < (1 << Q.nu1);
-    if (to_sel) __syncthreads();   // every group is done with its transpose buffers
-    for (int row = first; row <= last; row++) {
-        const uint32_t *src = ct + (row * 2 + g) * D;
-        uint32_t o[VPT];
-        ld16(o, src + zb);
-        if (upper) {
-            uint32_t nn[VPT];
-            ld16(nn, n1 + zb);
-#pragma unroll
-            for (int j = 0; j < VPT; j++) o[j] = reduce2(mont_mul(o[j], nn[j], c.p, c.pinv), c.p);
-        }
-#pragma unroll
-        for (int j = 0; j < VPT; j++) o[j] = canon4(o[j] + (row == 0 ? acc0[j] : acc1[j]), c.p);
-        if (row == 1) {
-#pragma unroll
-            for (int j = 0; j < VPT; j++) {
-                const int zs = auto_slot(zb + j, tau);
-                uint32_t tb = src[zs];
-                if (upper) tb = reduce2(mont_mul(tb, n1[zs], c.p, c.pinv), c.p);
-                o[j] = canon4(o[j] + tb, c.p);
-            }
-        }
-        if (r + 1 < Q.g) st16(Q.v[(r + 1) & 1] + (size_t)i * 4 * D + (row * 2 + g) * D + zb, o);
-        if (r == Q.capture && (i & 1) && (i / 2) < max_bits)
-            st16(Q.gsw_in + (size_t)(i / 2) * 4 * D + (row * 2 + g) * D + zb, o);
-        if (to_sel) st16(bufs + (row * 2 + g) * D + zb, o);
-    }
-    if (to_sel) {
-        __syncthreads();
-        uint4 *sl = reinterpret_cast<uint4 *>(Q.sel + (size_t)(i / 2) * D * 4);
-        for (int z = threadIdx.x; z < D; z += blockDim.x)
-            sl[z] = make_uint4(bufs[z], bufs[D + z], bufs[2 * D + z], bufs[3 * D + z]);
-    }
+    // GP = 2: group (g, sub) writes row `sub`
+    expand_store(Q, r, i, upper, ct, n1, tau, max_bits, GP == 2 ? sub : 0, GP == 2 ? sub : 1, g, t, c, bufs, acc0,
+                 acc1);
 }
 
 // Round r with many outputs: CTA blockIdx.x = parent p < 2^r of query
@@ -418,7 +429,6 @@ __global__ void __launch_bounds__(THREADS, 2) k_expand_pair(const QDesc *__restr
     const uint32_t *W = (left ? Q.left : Q.right) + (size_t)r * 2 * tk * 2 * D;
     const int bits = bits_per(tk);
     const uint32_t m32 = (uint32_t)((1ull << bits) - 1);
-    const int zb = VPT * t;
 #pragma unroll 1
     for (int h = 0; h < 2; h++) {
         const int i = pr + h * half;
@@ -459,42 +469,8 @@ __global__ void __launch_bounds__(THREADS, 2) k_expand_pair(const QDesc *__restr
             mac16(acc0, d, W + ((size_t)(0 * tk + k) * 2 + g) * D + VPT * t, c);
             mac16(acc1, d, W + ((size_t)(1 * tk + k) * 2 + g) * D + VPT * t, c);
         }
-        // output rows: row 0 = v.row0 + acc0, row 1 = v.row1 + acc1 + tau(v.row1),
         // v = c (lower child) or x^-k c (upper)
-        const bool to_sel = r == Q.g - 1 && !(i & 1) && (i / 2) < (1 << Q.nu1);
-        if (to_sel) __syncthreads();   // every group is done with its transpose buffers
-        for (int row = 0; row <= 1; row++) {
-            const uint32_t *src = ct + (row * 2 + g) * D;
-            uint32_t o[VPT];
-            ld16(o, src + zb);
-            if (upper) {
-                uint32_t nn[VPT];
-                ld16(nn, n1 + zb);
-#pragma unroll
-                for (int j = 0; j < VPT; j++) o[j] = reduce2(mont_mul(o[j], nn[j], c.p, c.pinv), c.p);
-            }
-#pragma unroll
-            for (int j = 0; j < VPT; j++) o[j] = canon4(o[j] + (row == 0 ? acc0[j] : acc1[j]), c.p);
-            if (row == 1) {
-#pragma unroll
-                for (int j = 0; j < VPT; j++) {
-                    const int zs = auto_slot(zb + j, tau);
-                    uint32_t tb = src[zs];
-                    if (upper) tb = reduce2(mont_mul(tb, n1[zs], c.p, c.pinv), c.p);
-                    o[j] = canon4(o[j] + tb, c.p);
-                }
-            }
-            if (r + 1 < Q.g) st16(Q.v[(r + 1) & 1] + (size_t)i * 4 * D + (row * 2 + g) * D + zb, o);
-            if (r == Q.capture && (i & 1) && (i / 2) < max_bits)
-                st16(Q.gsw_in + (size_t)(i / 2) * 4 * D + (row * 2 + g) * D + zb, o);
-            if (to_sel) st16(bufs + (row * 2 + g) * D + zb, o);
-        }
-        if (to_sel) {
-            __syncthreads();
-            uint4 *sl = reinterpret_cast<uint4 *>(Q.sel + (size_t)(i / 2) * D * 4);
-            for (int z = threadIdx.x; z < D; z += blockDim.x)
-                sl[z] = make_uint4(bufs[z], bufs[D + z], bufs[2 * D + z], bufs[3 * D + z]);
-        }
+        expand_store(Q, r, i, upper, ct, n1, tau, max_bits, 0, 1, g, t, c, bufs, acc0, acc1);
     }
 }
 
