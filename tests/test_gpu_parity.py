@@ -265,6 +265,26 @@ def test_fold(gpu):
     assert digest(got) == GOLDEN["fold"]["folded"]
 
 
+@pytest.mark.parametrize("pattern", ["v0_max", "v1_max", "all_max"])
+def test_fold_extreme_digits_match_oracle(gpu, pattern):
+    """Fold inputs whose gadget digits take extreme values: the first or the
+    second half of the columns (the two inputs of every level-0 fold) at
+    q - 1, the others 0, so the one-product fold's digit differences reach
+    both ends of [0, p) and its lazy digit transforms their largest inputs;
+    the result equals the oracle's two-product fold."""
+    T, nu2, t = 2, 3, 7
+    half = 1 << (nu2 - 1)
+    cts = np.zeros((T, 1 << nu2, 2, P.D), dtype=np.uint64)
+    if pattern in ("v0_max", "all_max"):
+        cts[:, :half] = P.Q - 1
+    if pattern in ("v1_max", "all_max"):
+        cts[:, half:] = P.Q - 1
+    V = seeded.residues(131, (nu2, 2, 2 * t))
+    got = gpu.fold(cts, V, nu2)
+    want = O.fold(cts, V, O.gsw_neg(V, t), nu2, t)
+    assert np.array_equal(got, want)
+
+
 def test_pack(gpu):
     x = cases.inputs("pack")
     gpu.set_client_keys(5, _keys_from(seeded.residues(1, (8, 2, 8)), seeded.residues(2, (6, 2, 8)),
