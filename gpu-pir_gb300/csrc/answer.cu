@@ -887,18 +887,58 @@ __device__ __forceinline__ uint32_t rescale_q(uint64_t x, int bits_out) {
     return (uint32_t)(neg ? ((0 - y) & mask) : y);
 }
 
+// The response: n*D values of q2_bits (row 0 of each column), then n*n*D
+// values of pt_bits + 2 (rows 1..n, row-major), least significant bit first
+// in little-endian 32-bit words.  A polynomial holds D * b = 64 * b words,
+// so each starts on a word boundary: first word of row a, column col.
+__device__ __forceinline__ uint32_t *poly_words(const QDesc &Q, const StageParams &sp, int a, int col) {
+    const size_t w0 = (size_t)(D / 32) * sp.q2_bits, w1 = (size_t)(D / 32) * (sp.pt_bits + 2);
+    const size_t w = a == 0 ? col * w0 : sp.n * w0 + (size_t)((a - 1) * sp.n + col) * w1;
+    return reinterpret_cast<uint32_t *>(Q.resp) + w;
+}
+
+// Raw coefficients of one response polynomial (this thread's layout-A
+// positions, the same in both groups) -> rescaled to b bits and serialised
+// into its 64 * b words at `out`.  Uses group 0's first transpose buffer;
+// ends with a CTA barrier.
+__device__ __forceinline__ void store_poly_bits(const Ctx &x, const uint64_t (&raw)[VPT], int b, uint32_t *out) {
+    uint32_t *vals = x.bufs;
+    if (x.g == 0) {
+#pragma unroll
+        for (int j = 0; j < VPT; j++) vals[x.t + GROUP * j] = rescale_q(raw[j], b);
+    }
+    __syncthreads();
+    const int words = (D / 32) * b;
+    for (int w = threadIdx.x; w < words; w += blockDim.x) {
+        const int lo = w * 32;
+        uint64_t acc = 0;
+        for (int e = lo / b; e < D && e * b < lo + 32; e++) {
+            const int off = e * b - lo;
+            const uint64_t v = vals[e];
+            acc |= off >= 0 ? (v << off) : (v >> -off);
+        }
+        out[w] = (uint32_t)acc;
+    }
+    __syncthreads();
+}
+
 // Column col of query blockIdx.y: sum over r < n of
 // W_r * NTT(G^-1(ct[r*n+col].row0)) + e_{1+r} * NTT(ct[r*n+col].row1), then
-// raw, then row 0 rescaled to 2^q2_bits and rows 1..n to 4p.
+// raw, then row 0 rescaled to 2^q2_bits and rows 1..n to 4p, serialised into
+// the response.
 // The n*(t_conv + 1) transforms of a column (digit k < t_conv of ct r's row
 // 0, or its row 1 for k = t_conv) are spread over `split` CTAs; with
 // split > 1 each CTA publishes its partial sums and the last to arrive
 // finishes the column (no CTA waits for another).  PACK_MAX_N (2 or 4) bounds
-// n: the n + 1 accumulators live in registers.
+// n: the n + 1 accumulators live in registers.  Launched in stream order
+// after every other kernel of the run: block (0, 0) passes the run's error
+// flag to h_err when given.
 template <int PACK_MAX_N>
 __global__ void __launch_bounds__(THREADS, PACK_MAX_N <= 2 ? 2 : 1) k_pack(const QDesc *__restrict__ qd, StageParams sp,
                                                  const TwiddleSet *__restrict__ tws, int split,
-                                                 uint32_t *__restrict__ part, unsigned int *__restrict__ counters) {
+                                                 uint32_t *__restrict__ part, unsigned int *__restrict__ counters,
+                                                 const int *__restrict__ d_err, int *__restrict__ h_err) {
+    if (h_err && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *h_err = *d_err;
     const QDesc &Q = qd[blockIdx.y];
     const int col = blockIdx.x / split, s = blockIdx.x % split;
     if (!Q.active || col >= sp.n) return;
@@ -979,17 +1019,105 @@ __global__ void __launch_bounds__(THREADS, PACK_MAX_N <= 2 ? 2 : 1) k_pack(const
         ntt_inv(acc[a], tw_inv(x), x.buf, c, x.t, x.bar);
         uint64_t raw[VPT];
         exchange_icrt(x, acc[a], raw);
-        const int ob = a == 0 ? sp.q2_bits : sp.pt_bits + 2;
-        uint32_t *o = Q.ms + ((size_t)a * n + col) * D;
-        if (x.g == 0) {
-#pragma unroll
-            for (int j = 0; j < VPT; j++) o[x.t + GROUP * j] = rescale_q(raw[j], ob);
-        }
+        store_poly_bits(x, raw, a == 0 ? sp.q2_bits : sp.pt_bits + 2, poly_words(Q, sp, a, col));
     }
 }
 
+// The pack when every response polynomial of the launch can have its own
+// SM: CTA blockIdx.x = item * split + s of query blockIdx.y computes only
+// row a of column col (item = a * n + col): the key products
+// W_r[a] * NTT(digit k of ct[r*n+col].row0) for r < n, k < t_conv, and for
+// a >= 1 the row 1 of ct[(a-1)*n+col] (the e_{1+r} term of k_pack).  Those
+// units are spread over `split` CTAs; the last to arrive sums the partials
+// and finishes the polynomial, so the n + 1 rows of a column finish on
+// different SMs at once instead of one after another.  One accumulator:
+// any n.  Launched in stream order; block (0, 0) passes the error flag.
+__global__ void __launch_bounds__(THREADS, 2) k_pack_row(const QDesc *__restrict__ qd, StageParams sp,
+                                                        const TwiddleSet *__restrict__ tws, int split,
+                                                        uint32_t *__restrict__ part,
+                                                        unsigned int *__restrict__ counters,
+                                                        const int *__restrict__ d_err, int *__restrict__ h_err) {
+    if (h_err && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *h_err = *d_err;
+    const QDesc &Q = qd[blockIdx.y];
+    const int n = sp.n, tcv = sp.t_conv, items = n * (n + 1);
+    const int item = blockIdx.x / split, s = blockIdx.x % split;
+    const int a = item / n, col = item % n;
+    if (!Q.active || item >= items) return;
+    extern __shared__ __align__(16) uint32_t smem[];
+    __shared__ int s_last;
+    const Ctx x = setup(smem, tws);
+    const Prime &c = x.c;
+    const int cols = 1 << Q.nu2;
+    const int bits = bits_per(tcv);
+    const uint64_t mask = (1ull << bits) - 1;
+    const int units = n * tcv + (a > 0);
+    uint32_t acc[VPT];
+#pragma unroll
+    for (int j = 0; j < VPT; j++) acc[j] = 0;
+#pragma unroll 1
+    for (int u = s; u < units; u += split) {
+        if (u < n * tcv) {
+            const int r = u / tcv, k = u % tcv;
+            const uint64_t *ct = Q.raw + (size_t)(r * n + col) * cols * 2 * D;
+            const uint32_t *W = Q.pack + (size_t)r * (n + 1) * tcv * 2 * D;
+            uint64_t raw[VPT];
+#pragma unroll
+            for (int j = 0; j < VPT; j++) raw[j] = ct[x.t + GROUP * j];
+            uint32_t d[VPT];
+            digits(d, raw, bits * k, mask);
+            ntt_fwd<1>(d, tw_fwd(x), x.buf, c, x.t, x.bar);
+            mac16(acc, d, W + ((size_t)(a * tcv + k) * 2 + x.g) * D + VPT * x.t, c);
+        } else {
+            const uint64_t *ct = Q.raw + (size_t)((a - 1) * n + col) * cols * 2 * D;
+            uint32_t b[VPT];
+#pragma unroll
+            for (int j = 0; j < VPT; j++) b[j] = mod_u64(ct[D + x.t + GROUP * j], c);
+            ntt_fwd(b, tw_fwd(x), x.buf, c, x.t, x.bar);
+#pragma unroll
+            for (int j = 0; j < VPT; j++) acc[j] = reduce2(acc[j] + reduce2(b[j], 2 * c.p), 2 * c.p);
+        }
+    }
+    if (split > 1) {
+        const size_t slot = (size_t)blockIdx.y * items + item;
+        auto plane = [&](int s2) { return part + ((slot * split + s2) * 2 + x.g) * D + VPT * x.t; };
+        st16(plane(s), acc);
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) s_last = atomicAdd(&counters[slot], 1u) == (unsigned)(split - 1);
+        __syncthreads();
+        if (!s_last) return;
+        __threadfence();
+        for (int s2 = 0; s2 < split; s2++) {
+            if (s2 == s) continue;
+            uint32_t w[VPT];
+            ld16_l2(w, plane(s2));
+#pragma unroll
+            for (int j = 0; j < VPT; j++) acc[j] = reduce2(acc[j] + w[j], 2 * c.p);
+        }
+        if (threadIdx.x == 0) counters[slot] = 0;   // ready for the next launch
+    }
+    ntt_inv(acc, tw_inv(x), x.buf, c, x.t, x.bar);
+    uint64_t raw[VPT];
+    exchange_icrt(x, acc, raw);
+    store_poly_bits(x, raw, a == 0 ? sp.q2_bits : sp.pt_bits + 2, poly_words(Q, sp, a, col));
+}
+
 cudaError_t launch_pack(const QDesc *qd, int nq, const StageParams &sp, const TwiddleSet *tw,
-                        const SplitScratch *scr, cudaStream_t st, int split_shift) {
+                        const SplitScratch *scr, cudaStream_t st, int split_shift, const int *d_err, int *h_err) {
+    const int sms = sm_count();
+    const uint64_t items = (uint64_t)sp.n * (sp.n + 1) * nq;
+    if (scr && scr->part && items <= (uint64_t)sms && items <= (uint64_t)scr->counter_slots) {
+        // one SM per response polynomial: spread each one's key products
+        const int units = sp.n * sp.t_conv + 1;
+        int split = shifted_split((int)std::min<uint64_t>(std::max<uint64_t>(1, sms / items), (uint64_t)units),
+                                  split_shift, units);
+        while (split > 1 && items * split * 2 > (uint64_t)scr->slots * 4) split--;
+        cudaError_t e = cudaFuncSetAttribute(k_pack_row, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        if (e != cudaSuccess) return e;
+        k_pack_row<<<dim3(sp.n * (sp.n + 1) * split, nq), THREADS, SMEM_BYTES, st>>>(qd, sp, tw, split, scr->part,
+                                                                                  scr->counters, d_err, h_err);
+        return cudaGetLastError();
+    }
     auto kernel = sp.n <= 2 ? k_pack<2> : k_pack<4>;
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     if (e != cudaSuccess) return e;
@@ -999,64 +1127,19 @@ cudaError_t launch_pack(const QDesc *qd, int nq, const StageParams &sp, const Tw
     const int units = sp.n * (sp.t_conv + 1);
     int split = 1;
     if (scr && scr->part) {
-        split = shifted_split((int)std::min<uint64_t>(std::max<uint64_t>(1, sm_count() / cols), (uint64_t)units),
+        split = shifted_split((int)std::min<uint64_t>(std::max<uint64_t>(1, sms / cols), (uint64_t)units),
                               split_shift, units);
         while (split > 1 && (cols * split * (sp.n + 1) * 2 > (uint64_t)scr->slots * 4 || cols > (uint64_t)scr->counter_slots))
             split--;
     }
     kernel<<<dim3(sp.n * split, nq), THREADS, SMEM_BYTES, st>>>(qd, sp, tw, split, scr ? scr->part : nullptr,
-                                                               scr ? scr->counters : nullptr);
+                                                               scr ? scr->counters : nullptr, d_err, h_err);
     return cudaGetLastError();
 }
 
 uint64_t response_bytes(const StageParams &sp) {
     const uint64_t bits = (uint64_t)sp.n * D * sp.q2_bits + (uint64_t)sp.n * sp.n * D * (sp.pt_bits + 2);
     return (bits + 63) / 64 * 8;
-}
-
-// Serialise: first n*D values of q2_bits, then n*n*D values of pt_bits+2,
-// least significant bit first, packed into little-endian 32-bit words.
-__global__ void k_bitpack(const QDesc *__restrict__ qd, StageParams sp, uint64_t words, const int *__restrict__ d_err,
-                          int *__restrict__ h_err) {
-    // every earlier kernel of the run has completed: pass on its error flag
-    if (h_err && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *h_err = *d_err;
-    const QDesc &Q = qd[blockIdx.y];
-    if (!Q.active) return;
-    const uint64_t n0 = (uint64_t)sp.n * D;
-    const uint64_t n1 = (uint64_t)sp.n * sp.n * D;
-    const int b0 = sp.q2_bits, b1 = sp.pt_bits + 2;
-    const uint64_t end0 = n0 * b0;
-    uint32_t *out = reinterpret_cast<uint32_t *>(Q.resp);
-    for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < words; w += (uint64_t)gridDim.x * blockDim.x) {
-        const uint64_t lo = w * 32, hi = lo + 32;
-        uint64_t acc = 0;
-        // section 0
-        if (lo < end0) {
-            uint64_t e = lo / b0;
-            for (; e < n0 && e * b0 < hi; e++) {
-                const int64_t off = (int64_t)(e * b0) - (int64_t)lo;
-                const uint64_t v = Q.ms[e];
-                acc |= off >= 0 ? (v << off) : (v >> (-off));
-            }
-        }
-        if (hi > end0) {
-            uint64_t e = lo > end0 ? (lo - end0) / b1 : 0;
-            for (; e < n1 && end0 + e * b1 < hi; e++) {
-                const int64_t off = (int64_t)(end0 + e * b1) - (int64_t)lo;
-                const uint64_t v = Q.ms[n0 + e];
-                acc |= off >= 0 ? (v << off) : (v >> (-off));
-            }
-        }
-        out[w] = (uint32_t)acc;
-    }
-}
-
-cudaError_t launch_bitpack(const QDesc *qd, int nq, const StageParams &sp, uint64_t resp_bytes, cudaStream_t st,
-                           const int *d_err, int *h_err) {
-    const uint64_t words = resp_bytes / 4;
-    int blocks = (int)((words + 255) / 256);
-    k_bitpack<<<dim3(blocks, nq), 256, 0, st>>>(qd, sp, words, d_err, h_err);
-    return cudaGetLastError();
 }
 
 }  // namespace sp

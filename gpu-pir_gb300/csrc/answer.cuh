@@ -53,12 +53,12 @@ cudaError_t launch_gsw_neg(const uint32_t *gsw, uint32_t *neg, int count, int t,
 // scr == nullptr: no split (every item in one CTA)
 cudaError_t launch_fold_level(const QDesc *qd, int nq, int level, int max_items, const StageParams &sp,
                               const TwiddleSet *tw, const SplitScratch *scr, cudaStream_t st, int split_shift = 0);
+// Pack, modulus switch and serialise each query's response to Q.resp (device
+// memory, or pinned host memory for runs with host I/O): one launch, after
+// every other kernel of the run; with h_err, it also copies *d_err to *h_err.
 cudaError_t launch_pack(const QDesc *qd, int nq, const StageParams &sp, const TwiddleSet *tw,
-                        const SplitScratch *scr, cudaStream_t st, int split_shift = 0);
-// Serialise each query's response to Q.resp (device memory, or pinned host
-// memory for runs with host I/O); with h_err, also copy *d_err to *h_err.
-cudaError_t launch_bitpack(const QDesc *qd, int nq, const StageParams &sp, uint64_t resp_bytes,
-                           cudaStream_t st, const int *d_err = nullptr, int *h_err = nullptr);
+                        const SplitScratch *scr, cudaStream_t st, int split_shift = 0, const int *d_err = nullptr,
+                        int *h_err = nullptr);
 // Descriptors h_qd[0, nq) (pinned host memory) to d_qd, and the u64 queries
 // h_query[nq][2][2][D] (pinned) narrowed into each descriptor's query planes.
 cudaError_t launch_stage_in(const QDesc *h_qd, QDesc *d_qd, const uint64_t *h_query, int nq, cudaStream_t st);

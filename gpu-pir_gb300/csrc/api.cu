@@ -349,7 +349,6 @@ uint64_t slot_layout(const sp_ctx *c, const Shape &s, uint8_t *base, Slot *sl, s
     q.gsw = (uint32_t *)take((uint64_t)s.nu2 * 2 * 2 * c->sp.t_gsw * 2 * D * 4, "slot GSW ciphertexts");
     q.acc = (uint32_t *)take(((uint64_t)T * ct) << s.nu2, "slot multiply output");
     q.raw = (uint64_t *)take(((uint64_t)T * 2 * D * 8) << s.nu2, "slot fold buffer");
-    q.ms = (uint32_t *)take((uint64_t)(c->sp.n + 1) * c->sp.n * D * 4, "slot modulus-switched response");
     q.resp = take(response_bytes(c->sp), "slot response bytes");
     if (sl) {
         sl->query32 = query32;
@@ -784,11 +783,10 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
         for (int lvl = 0; lvl < max_nu2 && !e; lvl++)
             e = launch_fold_level(L.d_qd, nq, lvl, sp.T << (max_nu2 - 1 - lvl), sp, c->d_tw, &L.split, st, cur_shift);
         if (!e) e = cudaEventRecordWithFlags(L.ev[4], st, ev_flags);
-        if (!e) e = launch_pack(L.d_qd, nq, sp, c->d_tw, &L.split, st, cur_shift);
         // with host I/O the responses (descriptors point into the pinned
         // staging) and the error flag go to host memory from the kernel
-        if (!e) e = launch_bitpack(L.d_qd, nq, sp, response_bytes(sp), st, io ? L.d_err : nullptr,
-                                   io ? L.h_err : nullptr);
+        if (!e) e = launch_pack(L.d_qd, nq, sp, c->d_tw, &L.split, st, cur_shift, io ? L.d_err : nullptr,
+                                io ? L.h_err : nullptr);
         if (!e) e = cudaEventRecordWithFlags(L.ev[5], st, ev_flags);
         return e;
     };
@@ -837,10 +835,13 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
     } else {
         CU(enqueue(false));
     }
-    uint64_t launches = (uint64_t)max_g + 1 + 1 + (uint64_t)max_nu2 + 2 + (io ? 1 : 0);
+    // expansion rounds, conversion, output to raw, fold levels, pack, and
+    // the staging kernel of runs with host I/O
+    uint64_t launches = (uint64_t)max_g + 1 + 1 + (uint64_t)max_nu2 + 1 + (io ? 1 : 0);
     for (const Group &gr : groups) {
         c->stats.db_mul_by_variant[gr.variant - 1]++;
-        launches += gr.variant == 3 ? 3 * (uint64_t)((gr.count + TC_MAX_Q - 1) / TC_MAX_Q) : 1;
+        launches += gr.variant == 3 ? (uint64_t)tc_launches(c->dbs.at(gr.db_id).L) * ((gr.count + TC_MAX_Q - 1) / TC_MAX_Q)
+                                    : 1;
     }
     c->stats.launches += launches;
     c->stats.db_mul_calls += groups.size();
@@ -1906,23 +1907,20 @@ int sp_pack(sp_ctx *c, int32_t client_id, const uint64_t *cts, uint8_t *response
     if (ci == c->clients.end()) return fail(SP_ERR_NOT_FOUND, "unknown client id");
     const uint64_t rb = response_bytes(c->sp);
     if (response_len < rb) return fail(SP_ERR_INVALID, "response buffer too small");
-    const int T = c->sp.T, n = c->sp.n;
-    Tmp r(c), ms(c), resp(c), qd(c);
+    const int T = c->sp.T;
+    Tmp r(c), resp(c), qd(c);
     TRY(r.get((uint64_t)T * 2 * D * 8));
-    TRY(ms.get((uint64_t)(n + 1) * n * D * 4));
     TRY(resp.get(rb));
     TRY(qd.get(sizeof(QDesc)));
     QDesc d{};
     d.pack = ci->second.pack;
     d.raw = r.as<uint64_t>();
-    d.ms = ms.as<uint32_t>();
     d.resp = resp.as<uint8_t>();
     d.nu2 = 0;   // one ciphertext per instance
     d.active = 1;
     CU(cudaMemcpyAsync(r.p, cts, (uint64_t)T * 2 * D * 8, cudaMemcpyHostToDevice, c->st));
     CU(cudaMemcpyAsync(qd.p, &d, sizeof(QDesc), cudaMemcpyHostToDevice, c->st));
     CU(launch_pack(qd.as<QDesc>(), 1, c->sp, c->d_tw, nullptr, c->st));
-    CU(launch_bitpack(qd.as<QDesc>(), 1, c->sp, rb, c->st));
     CU(cudaMemcpyAsync(response, resp.p, rb, cudaMemcpyDeviceToHost, c->st));
     CU(cudaStreamSynchronize(c->st));
     return verify_guards(c);

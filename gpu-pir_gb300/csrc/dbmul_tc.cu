@@ -600,6 +600,8 @@ static int tc_chunk(const DbLayout &L) {
 
 uint64_t tc_out_bytes(const DbLayout &L) { return 2ull * tc_chunk(L) * L.combos * TC_MAX_N * 4; }
 
+int tc_launches(const DbLayout &L) { return 1 + 2 * (D / tc_chunk(L)); }
+
 cudaError_t launch_db_mul_tc(const uint32_t *db, const DbLayout &L, const QDesc *qd, int nq, uint8_t *limbs,
                              uint32_t *out, int *err, cudaStream_t st) {
     if (!db_mul_tc_supported(L) || nq < 1 || nq > TC_MAX_Q) return cudaErrorInvalidValue;

@@ -94,7 +94,6 @@ struct QDesc {
     uint32_t *gsw;           // [nu2][2][2*t_gsw][2][D], Montgomery form
     uint32_t *acc;           // [T][cols][2][2][D]  DB-multiply output
     uint64_t *raw;           // [T][cols][2][D]     fold buffer
-    uint32_t *ms;            // [n+1][n][D]         modulus-switched response
     uint8_t *resp;           // response bytes
     int nu1, nu2, g, stop, capture;
     int active;
@@ -167,6 +166,9 @@ constexpr int TC_MAX_Q = 32;
 bool db_mul_tc_supported(const DbLayout &L);
 uint64_t tc_limb_bytes(const DbLayout &L);
 uint64_t tc_out_bytes(const DbLayout &L);
+// kernels one launch_db_mul_tc call launches: the digit split, then a
+// multiply and a transpose per chunk of slots
+int tc_launches(const DbLayout &L);
 cudaError_t launch_db_mul_tc(const uint32_t *db, const DbLayout &L, const QDesc *qd, int nq, uint8_t *limbs,
                              uint32_t *out, int *err, cudaStream_t st);
 
