@@ -293,6 +293,25 @@ def test_pack(gpu):
     assert digest(resp) == GOLDEN["pack"]["response"]
 
 
+@pytest.mark.parametrize("n,t_conv,pt_bits,q2_bits", [(1, 3, 4, 6), (2, 8, 8, 32), (4, 4, 8, 22)])
+def test_pack_across_n_matches_oracle(n, t_conv, pt_bits, q2_bits):
+    """The pack stage entry runs the batch pack kernel (one CTA group per
+    column, n + 1 accumulators in registers, serialisation by the CTA that
+    finishes each polynomial): response bytes equal the oracle's pack and
+    serialisation for n = 1, 2 and 4 and the extreme first-row widths.  The
+    row-per-CTA kernel that single queries use is covered at these n by
+    whole answers (test_gpu_param_sets.py)."""
+    p = _p(n=n, t_conv=t_conv, pt_bits=pt_bits, q2_bits=q2_bits)
+    cts = seeded.raw(130 + n, (n * n, 2))
+    keys = seeded.residues(140 + n, (n, n + 1, t_conv))
+    with SpiralGPU(p, max_batch=1) as g:
+        g.set_client_keys(1, _keys_from(seeded.residues(1, (8, 2, 8)), seeded.residues(2, (6, 2, 8)),
+                                        seeded.residues(3, (2, 2 * t_conv)), keys))
+        resp = g.pack(1, cts)
+    ref = O.encode_response(O.pack(cts, keys, n, t_conv), n, pt_bits, q2_bits)
+    assert np.array_equal(resp, ref)
+
+
 def test_answer_matches_oracle(gpu):
     """The whole pipeline on seeded (non-encrypted) inputs: response bytes are
     identical to the oracle's."""
