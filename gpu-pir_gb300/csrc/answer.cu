@@ -494,16 +494,15 @@ cudaError_t launch_expand_round(const QDesc *qd, int nq, int r, int max_out, con
                                 cudaStream_t st, int split_shift) {
     const uint64_t total = (uint64_t)max_out * nq;
     const int sms = sm_count();
-    const int force = expand_kernel_override();
-    if (force ? force == 1 : total < 2ull * sms) {
+    const int kernel = expand_kernel(max_out, nq, sms, expand_kernel_override());
+    if (kernel == EXPAND_SPLIT) {
         // few outputs: 2 groups per prime split the digits; with scratch,
         // each output also spreads over `split` CTAs while that stays within
         // one CTA per SM, at least one digit transform per group
         int split = 1;
         if (scr && scr->part) {
             const int digits = std::max(sp.t_left, sp.t_right);
-            split = shifted_split((int)std::min<uint64_t>(std::max<uint64_t>(1, sms / total), (uint64_t)(digits + 1) / 2),
-                                  split_shift, (digits + 1) / 2);
+            split = shifted_split(split_rule(sms, total, (digits + 1) / 2), split_shift, (digits + 1) / 2);
             while (split > 1 && (total * split > (uint64_t)scr->slots || total > (uint64_t)scr->counter_slots)) split--;
         }
         const int smem = (TW_WORDS + 4 * 2 * D) * 4 + D * 8;
@@ -514,9 +513,8 @@ cudaError_t launch_expand_round(const QDesc *qd, int nq, int r, int max_out, con
         if (e != cudaSuccess) return e;
     } else {
         const int smem = SMEM_BYTES + D * 8;
-        const uint64_t pairs = (uint64_t)std::max(1, max_out / 2) * nq;
         cudaError_t e;
-        if (force ? force == 3 : pairs >= 4ull * sms) {
+        if (kernel == EXPAND_PAIR) {
             // at least two waves of parents: one CTA per parent computes both
             // children (one inverse transform instead of two)
             e = cudaFuncSetAttribute(k_expand_pair, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -836,7 +834,7 @@ cudaError_t launch_fold_level(const QDesc *qd, int nq, int level, int max_items,
                               const TwiddleSet *tw, const SplitScratch *scr, cudaStream_t st, int split_shift) {
     const uint64_t total = (uint64_t)max_items * nq;
     const int sms = sm_count();
-    if (total <= (uint64_t)sms) {
+    if (fold_narrow(total, sms)) {
         // few folds (one CTA per SM): 2 groups per prime split the digits;
         // above that one 256-thread CTA per fold, two per SM, finishes a
         // level in one wave up to 2 x SMs folds.  With scratch, each
@@ -845,8 +843,7 @@ cudaError_t launch_fold_level(const QDesc *qd, int nq, int level, int max_items,
         // group
         int split = 1;
         if (scr && scr->part) {
-            split = shifted_split((int)std::min<uint64_t>(std::max<uint64_t>(1, sms / total), (uint64_t)sp.t_gsw),
-                                  split_shift, sp.t_gsw);
+            split = shifted_split(split_rule(sms, total, sp.t_gsw), split_shift, sp.t_gsw);
             while (split > 1 && (total * split > (uint64_t)scr->slots || total > (uint64_t)scr->counter_slots)) split--;
         }
         const int smem = (TW_WORDS + 4 * 2 * D) * 4;
@@ -1105,12 +1102,11 @@ __global__ void __launch_bounds__(THREADS, 2) k_pack_row(const QDesc *__restrict
 cudaError_t launch_pack(const QDesc *qd, int nq, const StageParams &sp, const TwiddleSet *tw,
                         const SplitScratch *scr, cudaStream_t st, int split_shift, const int *d_err, int *h_err) {
     const int sms = sm_count();
-    const uint64_t items = (uint64_t)sp.n * (sp.n + 1) * nq;
-    if (scr && scr->part && items <= (uint64_t)sms && items <= (uint64_t)scr->counter_slots) {
+    if (pack_by_row(sp.n, nq, sms, scr && scr->part, scr ? scr->counter_slots : 0)) {
         // one SM per response polynomial: spread each one's key products
+        const uint64_t items = (uint64_t)sp.n * (sp.n + 1) * nq;
         const int units = sp.n * sp.t_conv + 1;
-        int split = shifted_split((int)std::min<uint64_t>(std::max<uint64_t>(1, sms / items), (uint64_t)units),
-                                  split_shift, units);
+        int split = shifted_split(split_rule(sms, items, units), split_shift, units);
         while (split > 1 && items * split * 2 > (uint64_t)scr->slots * 4) split--;
         cudaError_t e = cudaFuncSetAttribute(k_pack_row, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
         if (e != cudaSuccess) return e;
@@ -1127,8 +1123,7 @@ cudaError_t launch_pack(const QDesc *qd, int nq, const StageParams &sp, const Tw
     const int units = sp.n * (sp.t_conv + 1);
     int split = 1;
     if (scr && scr->part) {
-        split = shifted_split((int)std::min<uint64_t>(std::max<uint64_t>(1, sms / cols), (uint64_t)units),
-                              split_shift, units);
+        split = shifted_split(split_rule(sms, cols, units), split_shift, units);
         while (split > 1 && (cols * split * (sp.n + 1) * 2 > (uint64_t)scr->slots * 4 || cols > (uint64_t)scr->counter_slots))
             split--;
     }

@@ -7,6 +7,7 @@
 // queries against databases of different shapes run in the same launch.
 #pragma once
 #include "kernels.cuh"
+#include "plan.h"
 
 namespace sp {
 
@@ -19,18 +20,6 @@ struct SplitScratch {
     uint32_t *counters = nullptr;   // [counter_slots], zero between launches
     int slots = 0, counter_slots = 0;
 };
-// Split schedules of the narrow launches (few items: an expansion round, a
-// fold level or the pack spreads each item over `split` CTAs).  The rule
-// gives split = min(SMs / items, cap); a schedule shifts it: shift s >= 0
-// multiplies it by 2^s, s < 0 divides it by 2^-s, SPLIT_NONE runs one CTA per
-// item; the result stays in [1, cap].  Chosen per batch class by the
-// autotuner (api.cu); every schedule gives the same residues.
-constexpr int SPLIT_NONE = -16;
-inline int shifted_split(int rule, int shift, int cap) {
-    if (shift <= SPLIT_NONE) return 1;
-    const int s = shift >= 0 ? rule << shift : rule >> -shift;
-    return s < 1 ? 1 : (s > cap ? cap : s);
-}
 
 // u64 canonical residues [count][2][D] -> u32 (optionally Montgomery form)
 cudaError_t launch_narrow(const uint64_t *in, uint32_t *out, uint64_t planes, bool to_mont, cudaStream_t st);

@@ -1986,15 +1986,11 @@ void finish_lane(sp_ctx *c, Lane &L) {
 void launch_lane(sp_ctx *c, Lane &L) {
     TraceRange trace_("serve_batch");
     std::vector<Pending> batch;
-    // A queue that fits in one batch runs whole, in arrival order.  A longer
-    // one runs by database: the oldest request's database first, with its
-    // other queued requests (up to the lane's capacity, in arrival order),
-    // so that one pass over a database image serves as many queries as are
-    // waiting for it; requests for other databases keep their place.
-    const bool by_db = (int)c->queue.size() > L.cap;
-    const int db_first = c->queue.empty() ? 0 : c->queue.front().db_id;
+    // batch policy (plan.h batch_rule): the whole queue in arrival order
+    // when it fits, else the oldest request's database first
+    const BatchRule rule = batch_rule(c->queue.size(), L.cap, c->queue.empty() ? 0 : c->queue.front().db_id);
     for (auto qi = c->queue.begin(); qi != c->queue.end() && (int)batch.size() < L.cap;) {
-        if (by_db && qi->db_id != db_first) {
+        if (!rule.takes(qi->db_id)) {
             ++qi;
             continue;
         }
