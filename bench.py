@@ -430,6 +430,24 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def stage_split(g, count: int, runs: int = 1) -> dict:
+    """The library's stats over `runs` staged runs of `count` queries with
+    its stage timing on (events between the stages), the ms_* fields per
+    run; two runs before them capture the timed plan's graph, and the timing
+    is off again afterwards (the timed headline runs without it)."""
+    g.set_stage_timing(True)
+    try:
+        for _ in range(2):
+            g.run_staged(count)
+        g.stats_reset()
+        for _ in range(runs):
+            g.run_staged(count)
+        st = g.stats()
+    finally:
+        g.set_stage_timing(False)
+    return {k: (v / runs if k.startswith("ms_") else v) for k, v in st.items()}
+
+
 def run_gpu(args, rank, world, local):
     from spiralpir.lib import SpiralGPU
 
@@ -469,11 +487,8 @@ def run_gpu(args, rank, world, local):
         ms = gpu.time_staged(batch, args.steps)
     st = gpu.stats()
     launches_per_answer = st["launches"] / max(1, args.steps)
-    # per-stage split: CUDA events inside three more staged runs
-    gpu.stats_reset()
-    for _ in range(3):
-        gpu.run_staged(batch)
-    split = gpu.stats()
+    # per-stage split: CUDA events between the stages of three more staged runs
+    split = stage_split(gpu, batch, runs=3)
     # first-dimension multiply alone (roofline): CUDA events around its launches
     with clocks.window():
         mul_ms = gpu.time_db_mul(1, batch, max(args.steps, 5))
@@ -513,9 +528,7 @@ def run_gpu(args, rank, world, local):
             gpu2.time_staged(B, 2)
             with clocks.window():
                 bms = gpu2.time_staged(B, max(2, args.steps // 4))
-            gpu2.stats_reset()
-            gpu2.run_staged(B)
-            bsplit = gpu2.stats()
+            bsplit = stage_split(gpu2, B)
             eq = dec = 0
             for s in range(B):
                 rb = gpu2.fetch_response(s)
@@ -583,7 +596,7 @@ def run_gpu(args, rank, world, local):
                          "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
                          "algorithmic_bytes_per_launch": algo_bytes, "launch_ms": mul_ms,
                          "traffic": traffic},
-            "stages_ms": {k[3:]: split[k] / 3 for k in
+            "stages_ms": {k[3:]: split[k] for k in
                           ("ms_expand", "ms_convert", "ms_db_mul", "ms_fold", "ms_pack", "ms_total")},
             "gpu_launches": int(st["launches"]), "launches_per_answer": launches_per_answer,
             "batched": batched, "clocks": clk, "db_load_s": load_s, "decoded_ok": ok}
@@ -672,9 +685,7 @@ def bench_uneven(p, cl, keys, recs1g, clocks) -> dict:
             g.time_staged(B, 2)
             with clocks.window():
                 ms = g.time_staged(B, 5)
-            g.stats_reset()
-            g.run_staged(B)
-            st = g.stats()
+            st = stage_split(g, B)
             batch = g.answer_batch(reqs)
             alone = [g.answer(*r) for r in reqs]
             eq = sum(bool(np.array_equal(a, b)) for a, b in zip(batch, alone))

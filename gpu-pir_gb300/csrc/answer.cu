@@ -540,11 +540,13 @@ cudaError_t launch_expand_round(const QDesc *qd, int nq, int r, int max_out, con
 // one is transformed.
 __global__ void __launch_bounds__(THREADS, 2) k_acc_to_raw(const QDesc *__restrict__ qd, StageParams sp,
                                                           const TwiddleSet *__restrict__ tws) {
+    pdl_launch_dependents();
     const QDesc &Q = qd[blockIdx.y];
     const int n_items = sp.T * (2 << Q.nu2);
     if (!Q.active || (int)blockIdx.x >= n_items) return;
     extern __shared__ __align__(16) uint32_t smem[];
-    const Ctx x = setup(smem, tws);
+    const Ctx x = setup(smem, tws);   // constant: may overlap the multiply's tail
+    pdl_wait();                       // the multiply's accumulators
     uint32_t next[VPT];
     ld16(next, Q.acc + ((size_t)blockIdx.x * 2 + x.g) * D + VPT * x.t);
     for (int item = blockIdx.x; item < n_items; item += gridDim.x) {
@@ -564,12 +566,13 @@ __global__ void __launch_bounds__(THREADS, 2) k_acc_to_raw(const QDesc *__restri
 }
 
 cudaError_t launch_acc_to_raw(const QDesc *qd, int nq, int max_items, const StageParams &sp,
-                              const TwiddleSet *tw, cudaStream_t st) {
+                              const TwiddleSet *tw, cudaStream_t st, bool pdl) {
     cudaError_t e = cudaFuncSetAttribute(k_acc_to_raw, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     if (e != cudaSuccess) return e;
     // two resident CTAs per SM over all queries
     const int per_query = std::max(1, std::min(max_items, 2 * sm_count() / std::max(1, nq)));
-    k_acc_to_raw<<<dim3(per_query, nq), THREADS, SMEM_BYTES, st>>>(qd, sp, tw);
+    e = launch_ex(k_acc_to_raw, dim3(per_query, nq), dim3(THREADS), (size_t)SMEM_BYTES, st, pdl, qd, sp, tw);
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 
@@ -831,7 +834,9 @@ __global__ void __launch_bounds__(256 * GP, 3 - GP) k_fold_level(const QDesc *__
 }
 
 cudaError_t launch_fold_level(const QDesc *qd, int nq, int level, int max_items, const StageParams &sp,
-                              const TwiddleSet *tw, const SplitScratch *scr, cudaStream_t st, int split_shift) {
+                              const TwiddleSet *tw, const SplitScratch *scr, cudaStream_t st, int split_shift,
+                              bool pdl_first) {
+    const bool pdl = level > 0 || pdl_first;
     const uint64_t total = (uint64_t)max_items * nq;
     const int sms = sm_count();
     if (fold_narrow(total, sms)) {
@@ -849,13 +854,13 @@ cudaError_t launch_fold_level(const QDesc *qd, int nq, int level, int max_items,
         const int smem = (TW_WORDS + 4 * 2 * D) * 4;
         cudaError_t e = cudaFuncSetAttribute(k_fold_level<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
         if (e != cudaSuccess) return e;
-        e = launch_ex(k_fold_level<2>, dim3(max_items * split, nq), dim3(512), smem, st, level > 0, qd, level, sp, tw,
+        e = launch_ex(k_fold_level<2>, dim3(max_items * split, nq), dim3(512), smem, st, pdl, qd, level, sp, tw,
                       split, scr ? scr->part : nullptr, scr ? scr->counters : nullptr);
         if (e != cudaSuccess) return e;
     } else {
         cudaError_t e = cudaFuncSetAttribute(k_fold_level<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
         if (e != cudaSuccess) return e;
-        e = launch_ex(k_fold_level<1>, dim3(max_items, nq), dim3(THREADS), (size_t)SMEM_BYTES, st, level > 0, qd, level,
+        e = launch_ex(k_fold_level<1>, dim3(max_items, nq), dim3(THREADS), (size_t)SMEM_BYTES, st, pdl, qd, level,
                       sp, tw, 1, (uint32_t *)nullptr, (unsigned int *)nullptr);
         if (e != cudaSuccess) return e;
     }
@@ -927,14 +932,15 @@ __device__ __forceinline__ void store_poly_bits(const Ctx &x, const uint64_t (&r
 // 0, or its row 1 for k = t_conv) are spread over `split` CTAs; with
 // split > 1 each CTA publishes its partial sums and the last to arrive
 // finishes the column (no CTA waits for another).  PACK_MAX_N (2 or 4) bounds
-// n: the n + 1 accumulators live in registers.  Launched in stream order
-// after every other kernel of the run: block (0, 0) passes the run's error
-// flag to h_err when given.
+// n: the n + 1 accumulators live in registers.  The last kernel of a run
+// (in stream order, or dependent on the last fold level): after the wait,
+// block (0, 0) passes the run's error flag to h_err when given.
 template <int PACK_MAX_N>
 __global__ void __launch_bounds__(THREADS, PACK_MAX_N <= 2 ? 2 : 1) k_pack(const QDesc *__restrict__ qd, StageParams sp,
                                                  const TwiddleSet *__restrict__ tws, int split,
                                                  uint32_t *__restrict__ part, unsigned int *__restrict__ counters,
                                                  const int *__restrict__ d_err, int *__restrict__ h_err) {
+    pdl_wait();
     if (h_err && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *h_err = *d_err;
     const QDesc &Q = qd[blockIdx.y];
     const int col = blockIdx.x / split, s = blockIdx.x % split;
@@ -1028,21 +1034,23 @@ __global__ void __launch_bounds__(THREADS, PACK_MAX_N <= 2 ? 2 : 1) k_pack(const
 // units are spread over `split` CTAs; the last to arrive sums the partials
 // and finishes the polynomial, so the n + 1 rows of a column finish on
 // different SMs at once instead of one after another.  One accumulator:
-// any n.  Launched in stream order; block (0, 0) passes the error flag.
+// any n.  The last kernel of a run: the twiddle load may overlap the last
+// fold level; after the wait, block (0, 0) passes the error flag.
 __global__ void __launch_bounds__(THREADS, 2) k_pack_row(const QDesc *__restrict__ qd, StageParams sp,
                                                         const TwiddleSet *__restrict__ tws, int split,
                                                         uint32_t *__restrict__ part,
                                                         unsigned int *__restrict__ counters,
                                                         const int *__restrict__ d_err, int *__restrict__ h_err) {
-    if (h_err && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *h_err = *d_err;
     const QDesc &Q = qd[blockIdx.y];
     const int n = sp.n, tcv = sp.t_conv, items = n * (n + 1);
     const int item = blockIdx.x / split, s = blockIdx.x % split;
     const int a = item / n, col = item % n;
-    if (!Q.active || item >= items) return;
     extern __shared__ __align__(16) uint32_t smem[];
     __shared__ int s_last;
-    const Ctx x = setup(smem, tws);
+    const Ctx x = setup(smem, tws);   // twiddles: constant, may overlap the last fold level
+    pdl_wait();
+    if (h_err && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *h_err = *d_err;
+    if (!Q.active || item >= items) return;
     const Prime &c = x.c;
     const int cols = 1 << Q.nu2;
     const int bits = bits_per(tcv);
@@ -1100,7 +1108,8 @@ __global__ void __launch_bounds__(THREADS, 2) k_pack_row(const QDesc *__restrict
 }
 
 cudaError_t launch_pack(const QDesc *qd, int nq, const StageParams &sp, const TwiddleSet *tw,
-                        const SplitScratch *scr, cudaStream_t st, int split_shift, const int *d_err, int *h_err) {
+                        const SplitScratch *scr, cudaStream_t st, int split_shift, const int *d_err, int *h_err,
+                        bool pdl) {
     const int sms = sm_count();
     if (pack_by_row(sp.n, nq, sms, scr && scr->part, scr ? scr->counter_slots : 0)) {
         // one SM per response polynomial: spread each one's key products
@@ -1110,8 +1119,9 @@ cudaError_t launch_pack(const QDesc *qd, int nq, const StageParams &sp, const Tw
         while (split > 1 && items * split * 2 > (uint64_t)scr->slots * 4) split--;
         cudaError_t e = cudaFuncSetAttribute(k_pack_row, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
         if (e != cudaSuccess) return e;
-        k_pack_row<<<dim3(sp.n * (sp.n + 1) * split, nq), THREADS, SMEM_BYTES, st>>>(qd, sp, tw, split, scr->part,
-                                                                                  scr->counters, d_err, h_err);
+        e = launch_ex(k_pack_row, dim3(sp.n * (sp.n + 1) * split, nq), dim3(THREADS), (size_t)SMEM_BYTES, st, pdl, qd,
+                      sp, tw, split, scr->part, scr->counters, d_err, h_err);
+        if (e != cudaSuccess) return e;
         return cudaGetLastError();
     }
     auto kernel = sp.n <= 2 ? k_pack<2> : k_pack<4>;
@@ -1127,8 +1137,9 @@ cudaError_t launch_pack(const QDesc *qd, int nq, const StageParams &sp, const Tw
         while (split > 1 && (cols * split * (sp.n + 1) * 2 > (uint64_t)scr->slots * 4 || cols > (uint64_t)scr->counter_slots))
             split--;
     }
-    kernel<<<dim3(sp.n * split, nq), THREADS, SMEM_BYTES, st>>>(qd, sp, tw, split, scr ? scr->part : nullptr,
-                                                               scr ? scr->counters : nullptr, d_err, h_err);
+    e = launch_ex(kernel, dim3(sp.n * split, nq), dim3(THREADS), (size_t)SMEM_BYTES, st, pdl, qd, sp, tw, split,
+                  scr ? scr->part : nullptr, scr ? scr->counters : nullptr, d_err, h_err);
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 

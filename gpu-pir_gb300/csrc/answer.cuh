@@ -26,9 +26,13 @@ cudaError_t launch_narrow(const uint64_t *in, uint32_t *out, uint64_t planes, bo
 // u32 [count][2][D] (optionally from Montgomery form) -> u64 canonical
 cudaError_t launch_widen(const uint32_t *in, uint64_t *out, uint64_t planes, bool from_mont, cudaStream_t st);
 
+// The `pdl` flags below launch a kernel dependent on the previous kernel of
+// the stream (programmatic dependent launch): it starts as that one's CTAs
+// retire and waits for it to complete before reading its outputs.
+
 // DB-multiply output (NTT form) -> raw fold input, every query of qd
 cudaError_t launch_acc_to_raw(const QDesc *qd, int nq, int max_items, const StageParams &sp,
-                              const TwiddleSet *tw, cudaStream_t st);
+                              const TwiddleSet *tw, cudaStream_t st, bool pdl = false);
 // selectors u64 [rows][2 rows][2][D] -> device selector layout u32 [rows][D][4]
 cudaError_t launch_sel_import(const uint64_t *in, uint32_t *sel, int rows, cudaStream_t st);
 
@@ -39,15 +43,17 @@ cudaError_t launch_regev_to_gsw(const QDesc *qd, int nq, int max_items, const St
                                 const TwiddleSet *tw, cudaStream_t st);
 // G - C for count GSW ciphertexts (canonical in and out)
 cudaError_t launch_gsw_neg(const uint32_t *gsw, uint32_t *neg, int count, int t, cudaStream_t st);
-// scr == nullptr: no split (every item in one CTA)
+// scr == nullptr: no split (every item in one CTA).  Levels after the first
+// are dependent launches; the first one too with pdl_first.
 cudaError_t launch_fold_level(const QDesc *qd, int nq, int level, int max_items, const StageParams &sp,
-                              const TwiddleSet *tw, const SplitScratch *scr, cudaStream_t st, int split_shift = 0);
+                              const TwiddleSet *tw, const SplitScratch *scr, cudaStream_t st, int split_shift = 0,
+                              bool pdl_first = false);
 // Pack, modulus switch and serialise each query's response to Q.resp (device
 // memory, or pinned host memory for runs with host I/O): one launch, after
 // every other kernel of the run; with h_err, it also copies *d_err to *h_err.
 cudaError_t launch_pack(const QDesc *qd, int nq, const StageParams &sp, const TwiddleSet *tw,
                         const SplitScratch *scr, cudaStream_t st, int split_shift = 0, const int *d_err = nullptr,
-                        int *h_err = nullptr);
+                        int *h_err = nullptr, bool pdl = false);
 // Descriptors h_qd[0, nq) (pinned host memory) to d_qd, and the u64 queries
 // h_query[nq][2][2][D] (pinned) narrowed into each descriptor's query planes.
 cudaError_t launch_stage_in(const QDesc *h_qd, QDesc *d_qd, const uint64_t *h_query, int nq, cudaStream_t st);

@@ -121,6 +121,7 @@ struct Lane {
     uint64_t *h_query = nullptr; // pinned query staging [cap][2 rows][2 primes][D]
     int *h_err = nullptr;        // pinned copy of d_err
     cudaEvent_t ev[6]{};
+    bool ev_stages = false;             // the last run recorded ev[1..4] (stage timing)
     cudaEvent_t done = nullptr;
     // side stream of the Regev->GSW conversion, forked from the expansion
     // once its GSW-bit outputs are complete and joined before the folds
@@ -190,6 +191,10 @@ struct sp_ctx {
     std::map<std::vector<int64_t>, int> plan_split;
     std::deque<std::string> tune_log;
     bool use_graphs = true;     // replay the answer pipeline as CUDA graphs
+    // per-stage device time (sp_set_stage_timing): events between the
+    // stages of each run, at about 5 us each; off, the stages follow one
+    // another as dependent launches and only the run's total is timed
+    bool stage_timing = false;
     // serving (continuous batching)
     std::vector<Lane *> lanes;
     std::thread worker;
@@ -570,7 +575,8 @@ bool variant_available(sp_ctx *c, Lane &L, const Db &db, int nq, int variant) {
 }
 
 // Enqueue the multiply of `nq` queries (descriptors qd) against `db`.
-cudaError_t launch_mul_variant(Lane &L, const Db &db, const QDesc *qd, int nq, int variant) {
+// pdl: the per-query kernel as a dependent launch of the previous kernel
+cudaError_t launch_mul_variant(Lane &L, const Db &db, const QDesc *qd, int nq, int variant, bool pdl = false) {
     switch (variant) {
         case 2: return launch_db_mul_batch(db.d, db.L, qd, nq, L.st);
         case 3:
@@ -580,7 +586,7 @@ cudaError_t launch_mul_variant(Lane &L, const Db &db, const QDesc *qd, int nq, i
                 if (e != cudaSuccess) return e;
             }
             return cudaSuccess;
-        default: return launch_db_mul(db.d, db.L, qd, nq, L.d_err, L.st);
+        default: return launch_db_mul(db.d, db.L, qd, nq, L.d_err, L.st, pdl);
     }
 }
 
@@ -700,7 +706,8 @@ int tune_split(sp_ctx *c, Lane &L, const std::vector<int64_t> &key, Enqueue &enq
 // addresses directly) and its last writes the responses to L.h_resp (the
 // descriptors point there) and the error flag to L.h_err: no copies in the
 // captured graph.
-// Records stage events.
+// Records the run's first and last events, and with stage timing the stage
+// boundaries between them.
 //
 // The launches depend only on the batch plan: query count, the largest
 // expansion depth / fold depth / conversion size, and per run of slots on one
@@ -726,7 +733,8 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
         int db_id, begin, count, variant;
     };
     std::vector<Group> groups;
-    std::vector<int64_t> key = {nq, max_g, max_nu2, max_items, io ? 1 : 0};
+    const bool timed = c->stage_timing;
+    std::vector<int64_t> key = {nq, max_g, max_nu2, max_items, io ? 1 : 0, timed ? 1 : 0};
     uint64_t mul_bytes = 0;
     if (io) {
         // the autotuner times multiply launches on the staged descriptors:
@@ -753,7 +761,10 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
         i = j;
     }
     // stage events are recorded as external event nodes so that a replayed
-    // graph records them too
+    // graph records them too.  Without stage timing there is no event between
+    // stages and each stage's first kernel is a dependent launch of the
+    // previous stage's last (its constant loads overlap that one's tail; a
+    // per-query multiply streams the image before the selectors are ready)
     int cur_shift = 0;
     auto enqueue = [&](bool capturing) -> cudaError_t {
         const unsigned ev_flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
@@ -771,22 +782,25 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
                 if (!e) e = cudaEventRecord(L.join_ev, L.side);
             }
         }
-        if (!e) e = cudaEventRecordWithFlags(L.ev[1], st, ev_flags);
-        if (!e) e = cudaEventRecordWithFlags(L.ev[2], st, ev_flags);   // conversion: off the critical path
-        for (const Group &gr : groups) {
-            if (e) break;
-            e = launch_mul_variant(L, c->dbs.at(gr.db_id), L.d_qd + gr.begin, gr.count, gr.variant);
+        if (!e && timed) e = cudaEventRecordWithFlags(L.ev[1], st, ev_flags);
+        // the folds need the GSW ciphertexts: join the conversion here, where
+        // it has long finished (it overlaps the last expansion rounds)
+        if (!e) e = cudaStreamWaitEvent(st, L.join_ev, 0);
+        if (!e && timed) e = cudaEventRecordWithFlags(L.ev[2], st, ev_flags);   // conversion past the expansion
+        for (size_t k = 0; k < groups.size() && !e; k++) {
+            const Group &gr = groups[k];
+            e = launch_mul_variant(L, c->dbs.at(gr.db_id), L.d_qd + gr.begin, gr.count, gr.variant, !timed && k == 0);
         }
-        if (!e) e = cudaEventRecordWithFlags(L.ev[3], st, ev_flags);
-        if (!e) e = launch_acc_to_raw(L.d_qd, nq, sp.T * (2 << max_nu2), sp, c->d_tw, st);
-        if (!e) e = cudaStreamWaitEvent(st, L.join_ev, 0);   // the folds need the GSW ciphertexts
+        if (!e && timed) e = cudaEventRecordWithFlags(L.ev[3], st, ev_flags);
+        if (!e) e = launch_acc_to_raw(L.d_qd, nq, sp.T * (2 << max_nu2), sp, c->d_tw, st, !timed);
         for (int lvl = 0; lvl < max_nu2 && !e; lvl++)
-            e = launch_fold_level(L.d_qd, nq, lvl, sp.T << (max_nu2 - 1 - lvl), sp, c->d_tw, &L.split, st, cur_shift);
-        if (!e) e = cudaEventRecordWithFlags(L.ev[4], st, ev_flags);
+            e = launch_fold_level(L.d_qd, nq, lvl, sp.T << (max_nu2 - 1 - lvl), sp, c->d_tw, &L.split, st, cur_shift,
+                                  true);
+        if (!e && timed) e = cudaEventRecordWithFlags(L.ev[4], st, ev_flags);
         // with host I/O the responses (descriptors point into the pinned
         // staging) and the error flag go to host memory from the kernel
         if (!e) e = launch_pack(L.d_qd, nq, sp, c->d_tw, &L.split, st, cur_shift, io ? L.d_err : nullptr,
-                                io ? L.h_err : nullptr);
+                                io ? L.h_err : nullptr, !timed);
         if (!e) e = cudaEventRecordWithFlags(L.ev[5], st, ev_flags);
         return e;
     };
@@ -835,6 +849,7 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
     } else {
         CU(enqueue(false));
     }
+    L.ev_stages = timed;
     // expansion rounds, conversion, output to raw, fold levels, pack, and
     // the staging kernel of runs with host I/O
     uint64_t launches = (uint64_t)max_g + 1 + 1 + (uint64_t)max_nu2 + 1 + (io ? 1 : 0);
@@ -851,8 +866,9 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
 }
 
 int collect_stats(sp_ctx *c, Lane &L) {
-    float ms[5], tot;
-    for (int i = 0; i < 5; i++) CU(cudaEventElapsedTime(&ms[i], L.ev[i], L.ev[i + 1]));
+    float ms[5] = {0, 0, 0, 0, 0}, tot;
+    if (L.ev_stages)
+        for (int i = 0; i < 5; i++) CU(cudaEventElapsedTime(&ms[i], L.ev[i], L.ev[i + 1]));
     CU(cudaEventElapsedTime(&tot, L.ev[0], L.ev[5]));
     c->stats.ms_expand += ms[0];
     c->stats.ms_convert += ms[1];
@@ -1587,6 +1603,14 @@ int sp_set_graphs(sp_ctx *c, int32_t on) {
     std::lock_guard<std::mutex> lk(c->mu);
     TraceRange trace_("sp_set_graphs");
     c->use_graphs = on != 0;
+    return SP_OK;
+}
+
+int sp_set_stage_timing(sp_ctx *c, int32_t on) {
+    if (!c) return fail(SP_ERR_INVALID, "NULL context");
+    std::lock_guard<std::mutex> lk(c->mu);
+    TraceRange trace_("sp_set_stage_timing");
+    c->stage_timing = on != 0;
     return SP_OK;
 }
 

@@ -208,6 +208,10 @@ __host__ __device__ inline int mul_units_per_cta(const DbLayout &L) {
 // an arrival on its `empty` barrier, so only the producer waits for the
 // slowest warp.  At the end of each unit the row phases are summed (warp
 // shuffles, then through shared memory) and the unit's outputs written.
+// As a dependent launch (after the expansion) the producer starts streaming
+// the image at once, since the image does not depend on earlier kernels;
+// the consumers wait for the previous kernel before reading the descriptor
+// and the selectors.
 __global__ void __launch_bounds__(MUL_THREADS + 32, 2) k_db_mul(const uint32_t *__restrict__ db, DbLayout L,
                                                         const QDesc *__restrict__ qd, int *err) {
     extern __shared__ __align__(128) uint8_t smem_mul[];
@@ -218,8 +222,7 @@ __global__ void __launch_bounds__(MUL_THREADS + 32, 2) k_db_mul(const uint32_t *
     uint2 *red = reinterpret_cast<uint2 *>(smem_mul + 128 + mul_sel_bytes(L));   // [warp][cbp]
     uint8_t *stages = smem_mul + 128 + mul_sel_bytes(L) + MUL_WARPS * L.cbp * 8;
 
-    const QDesc &Q = qd[blockIdx.y];
-    const uint32_t *__restrict__ sel = Q.sel;
+    pdl_launch_dependents();
     const int U = mul_units_per_cta(L);
     const uint64_t u0 = (uint64_t)blockIdx.x * U;
     const int rows = L.rows, cb = L.cb, cbp = L.cbp, rw = L.rw;
@@ -257,6 +260,9 @@ __global__ void __launch_bounds__(MUL_THREADS + 32, 2) k_db_mul(const uint32_t *
         return;
     }
     // ---------------------------------------------------------- consumers
+    pdl_wait();   // the selectors come from the previous kernel
+    const QDesc &Q = qd[blockIdx.y];
+    const uint32_t *__restrict__ sel = Q.sel;
     auto consumers_sync = []() { asm volatile("bar.sync 1, %0;" ::"n"(MUL_THREADS) : "memory"); };
     const int groups = cbp / 8;                // threads per row
     const int mg = threadIdx.x % groups, rp = threadIdx.x / groups, RS = MUL_THREADS / groups;
@@ -351,7 +357,7 @@ __global__ void __launch_bounds__(MUL_THREADS + 32, 2) k_db_mul(const uint32_t *
 }
 
 cudaError_t launch_db_mul(const uint32_t *db, const DbLayout &L, const QDesc *qd, int nq, int *err,
-                          cudaStream_t st) {
+                          cudaStream_t st, bool pdl) {
     const int SR = mul_stage_rows(L);
     if (L.rows % SR != 0 || ((uint64_t)SR * L.rw * 4) % 16 != 0 || MUL_THREADS % (L.cbp / 8) != 0)
         return cudaErrorInvalidValue;
@@ -360,8 +366,18 @@ cudaError_t launch_db_mul(const uint32_t *db, const DbLayout &L, const QDesc *qd
     const int smem = mul_smem_bytes(L);
     cudaError_t e = cudaFuncSetAttribute(k_db_mul, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    dim3 grid((unsigned)ctas, nq);
-    k_db_mul<<<grid, MUL_THREADS + 32, smem, st>>>(db, L, qd, err);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)ctas, nq);
+    cfg.blockDim = dim3(MUL_THREADS + 32);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    e = cudaLaunchKernelEx(&cfg, k_db_mul, db, L, qd, err);
+    if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }
 

@@ -148,9 +148,11 @@ cudaError_t launch_db_import(const uint32_t *planes, const DbLayout &L, uint32_t
 // First-dimension multiply for the `nq` queries qd[0..nq) against one
 // database: reads qd[q].sel (u32[rows][D][4], row0 q1, row0 q2, row1 q1,
 // row1 q2) and writes qd[q].acc (u32[T][cols][2 rows][2][D]), canonical.
-// Streams the image once per query (bandwidth-bound variant).
+// Streams the image once per query (bandwidth-bound variant).  With pdl,
+// launched dependent on the previous kernel of the stream (programmatic
+// dependent launch): its image stream starts before that kernel ends.
 cudaError_t launch_db_mul(const uint32_t *db, const DbLayout &L, const QDesc *qd, int nq, int *err,
-                          cudaStream_t st);
+                          cudaStream_t st, bool pdl = false);
 // Same result, reading each database residue once per group of 8 queries
 // on the integer pipe (compute-bound variant).
 bool db_mul_batch_supported(const DbLayout &L);

@@ -101,6 +101,7 @@ _SIGS = {
     "sp_db_mul": [_P, _I, _P, _P],
     "sp_db_mul_batch": [_P, _I, _I, _P, _P],
     "sp_set_graphs": [_P, _I],
+    "sp_set_stage_timing": [_P, _I],
     "sp_db_save": [_P, _I, ctypes.c_char_p],
     "sp_db_restore": [_P, _I, ctypes.c_char_p],
     "sp_fold": [_P, _P, _P, _I, _I, _P],
@@ -292,6 +293,12 @@ class SpiralGPU:
         """Replay the answer pipeline as CUDA graphs (default) or launch its
         kernels one by one."""
         _check(self.lib.sp_set_graphs(self.h, 1 if on else 0))
+
+    def set_stage_timing(self, on: bool) -> None:
+        """Per-stage device time in stats() (ms_expand .. ms_pack): an event
+        between every two stages of each answer run (off by default, when
+        only ms_total is measured and the stages run as dependent launches)."""
+        _check(self.lib.sp_set_stage_timing(self.h, 1 if on else 0))
 
     def stats(self) -> dict:
         s = SpStats()

@@ -57,12 +57,13 @@ typedef struct sp_params {
     int32_t max_batch;   /* queries answered concurrently (workspace slots) */
 } sp_params;
 
-/* Per-stage device time accumulated since the last sp_stats_reset. */
+/* Per-stage device time accumulated since the last sp_stats_reset (the
+ * stage fields only for runs with stage timing on: sp_set_stage_timing). */
 typedef struct sp_stats_out {
     uint64_t answers;        /* queries answered */
     uint64_t launches;       /* kernel launches issued by answers */
     double ms_expand;        /* coefficient expansion */
-    double ms_convert;       /* Regev->GSW conversion */
+    double ms_convert;       /* Regev->GSW conversion past the expansion (join) */
     double ms_db_mul;        /* first-dimension multiply */
     double ms_fold;          /* DB output to raw + folding */
     double ms_pack;          /* packing, modulus switch, serialisation */
@@ -196,6 +197,14 @@ int sp_set_db_mul_variant(sp_ctx *ctx, int32_t variant);
  * and replayed.  Off: the same launches are issued one by one.  Reloading a
  * database drops the captured graphs.  No counterpart in the reference. */
 int sp_set_graphs(sp_ctx *ctx, int32_t on);
+/* Per-stage device time in sp_stats (default off).  On: each answer run
+ * records an event between every two stages (expansion, conversion join,
+ * multiply, output to raw + folds, pack), about 5 us each, and sp_stats
+ * accumulates ms_expand .. ms_pack.  Off: those fields stay 0, ms_total is
+ * still measured, and each stage's first kernel starts as a dependent launch
+ * of the previous stage's last.  The responses are identical.  No
+ * counterpart in the reference. */
+int sp_set_stage_timing(sp_ctx *ctx, int32_t on);
 /* Serving loop (continuous batching).  sp_serve_start starts a worker thread
  * with `lanes` pipeline lanes (each its own stream and max_batch workspace
  * slots).  sp_submit copies the request's query and returns a ticket; the

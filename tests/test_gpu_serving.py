@@ -77,6 +77,32 @@ def test_graph_replay_matches_direct_launches(world):
             assert np.array_equal(x, y)
 
 
+@pytest.mark.parametrize("variant", [1, 2])
+def test_stage_timing_on_and_off_match_alone(world, variant):
+    """With stage timing on (events between the stages) and off (the stages
+    as dependent launches, per-query multiply included), plain launches and
+    graph replays give every response of the query alone; the stage fields
+    of the stats fill only with the timing on."""
+    gpu, _, reqs, alone = world
+    batch = [(c, d, q) for c, d, q, _, _ in reqs[:8]]
+    gpu.set_db_mul_variant(variant)
+    try:
+        for timing in (True, False):
+            gpu.set_stage_timing(timing)
+            gpu.stats_reset()
+            for _ in range(3):   # plain launches, capture, replay
+                got = gpu.answer_batch(batch)
+                for x, y in zip(got, alone[:8]):
+                    assert np.array_equal(x, y)
+            st = gpu.stats()
+            assert st["ms_total"] > 0
+            stages = sum(st[k] for k in ("ms_expand", "ms_db_mul", "ms_fold", "ms_pack"))
+            assert (stages > 0) == timing
+    finally:
+        gpu.set_stage_timing(False)
+        gpu.set_db_mul_variant(0)
+
+
 def test_graphs_dropped_when_database_reloaded():
     """A captured plan refers to the database image; reloading the database
     under the same id must not replay stale pointers."""
