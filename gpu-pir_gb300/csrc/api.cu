@@ -768,8 +768,11 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
     int cur_shift = 0;
     auto enqueue = [&](bool capturing) -> cudaError_t {
         const unsigned ev_flags = capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+        // a captured graph holds events only with stage timing; otherwise the
+        // run's first and last events go on the stream around the graph
+        const bool run_ev = timed || !capturing;
         cudaError_t e = io ? enqueue_inputs(L, nq, st) : cudaSuccess;
-        if (!e) e = cudaEventRecordWithFlags(L.ev[0], st, ev_flags);
+        if (!e && run_ev) e = cudaEventRecordWithFlags(L.ev[0], st, ev_flags);
         for (int r = 0; r < max_g && !e; r++) {
             e = launch_expand_round(L.d_qd, nq, r, 2 << r, sp, c->d_tw, c->d_neg1, &L.split, st, cur_shift);
             if (!e && r == fork_round) {
@@ -801,7 +804,7 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
         // staging) and the error flag go to host memory from the kernel
         if (!e) e = launch_pack(L.d_qd, nq, sp, c->d_tw, &L.split, st, cur_shift, io ? L.d_err : nullptr,
                                 io ? L.h_err : nullptr, !timed);
-        if (!e) e = cudaEventRecordWithFlags(L.ev[5], st, ev_flags);
+        if (!e && run_ev) e = cudaEventRecordWithFlags(L.ev[5], st, ev_flags);
         return e;
     };
     // split schedule: forced, tuned earlier for this batch class, or tuned
@@ -845,7 +848,9 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
             if (e3 != cudaSuccess) return fail(SP_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e3));
             it = L.graphs.emplace(key, exec).first;
         }
+        if (!timed) CU(cudaEventRecord(L.ev[0], st));
         CU(cudaGraphLaunch(it->second, st));
+        if (!timed) CU(cudaEventRecord(L.ev[5], st));
     } else {
         CU(enqueue(false));
     }
