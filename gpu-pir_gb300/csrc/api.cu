@@ -124,7 +124,7 @@ struct Lane {
     bool ev_stages = false;             // the last run recorded ev[1..4] (stage timing)
     cudaEvent_t done = nullptr;
     // side stream of the Regev->GSW conversion, forked from the expansion
-    // once its GSW-bit outputs are complete and joined before the folds
+    // once its GSW-bit outputs are complete and joined before the multiply
     cudaStream_t side = nullptr;
     cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     int *d_err = nullptr;
@@ -777,8 +777,7 @@ int run_pipeline(sp_ctx *c, Lane &L, int nq, const std::vector<int> &db_of_slot,
             e = launch_expand_round(L.d_qd, nq, r, 2 << r, sp, c->d_tw, c->d_neg1, &L.split, st, cur_shift);
             if (!e && r == fork_round) {
                 // the conversion needs only the GSW-bit encodings: run it on
-                // the side stream, overlapping the remaining rounds and the
-                // multiply
+                // the side stream, overlapping the remaining rounds
                 e = cudaEventRecord(L.fork_ev, st);
                 if (!e) e = cudaStreamWaitEvent(L.side, L.fork_ev, 0);
                 if (!e) e = launch_regev_to_gsw(L.d_qd, nq, max_items, sp, c->d_tw, L.side);
