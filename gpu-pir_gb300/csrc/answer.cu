@@ -492,6 +492,8 @@ int expand_kernel_override() {
 cudaError_t launch_expand_round(const QDesc *qd, int nq, int r, int max_out, const StageParams &sp,
                                 const TwiddleSet *tw, const uint32_t *neg1, const SplitScratch *scr,
                                 cudaStream_t st, int split_shift) {
+    // round 0 is an ordinary launch: the dependent launches after it read
+    // their descriptors before their dependency wait (common.cuh)
     const uint64_t total = (uint64_t)max_out * nq;
     const int sms = sm_count();
     const int kernel = expand_kernel(max_out, nq, sms, expand_kernel_override());

@@ -367,6 +367,10 @@ __device__ __forceinline__ void load_twiddles(uint32_t *dst, const TwiddleSet *s
 // predecessor touches (the predecessor then has completed and its writes are
 // visible).  pdl_launch_dependents() lets the next such kernel start early.
 // Both are no-ops for a kernel launched the ordinary way.
+// In an answer run the first expansion round is an ordinary launch, so it
+// starts after the kernel that uploads the query descriptors has completed;
+// every later kernel of the run starts after that round has, and may read
+// its descriptor (for early exits) before its pdl_wait().
 __device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
