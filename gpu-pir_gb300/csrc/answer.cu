@@ -20,24 +20,6 @@ constexpr int THREADS = 256;
 constexpr int SMEM_WORDS = TW_WORDS + 2 * 2 * D;
 constexpr int SMEM_BYTES = SMEM_WORDS * 4;
 
-// Launch with programmatic stream serialisation when `pdl` (the kernel then
-// calls pdl_wait() before touching its predecessor's data), else normally.
-template <typename... KArgs, typename... Args>
-cudaError_t launch_ex(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool pdl,
-                      Args &&...args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = grid;
-    cfg.blockDim = block;
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = pdl ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
-}
-
 struct Ctx {
     const uint32_t *tw;   // 2 tables (TW_WORDS words)
     uint32_t *buf;   // this group's two transpose buffers

@@ -366,17 +366,7 @@ cudaError_t launch_db_mul(const uint32_t *db, const DbLayout &L, const QDesc *qd
     const int smem = mul_smem_bytes(L);
     cudaError_t e = cudaFuncSetAttribute(k_db_mul, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)ctas, nq);
-    cfg.blockDim = dim3(MUL_THREADS + 32);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = pdl ? 1 : 0;
-    e = cudaLaunchKernelEx(&cfg, k_db_mul, db, L, qd, err);
+    e = launch_ex(k_db_mul, dim3((unsigned)ctas, nq), dim3(MUL_THREADS + 32), (size_t)smem, st, pdl, db, L, qd, err);
     if (e != cudaSuccess) return e;
     return cudaGetLastError();
 }

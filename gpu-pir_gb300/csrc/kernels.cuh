@@ -4,9 +4,29 @@
 #include <stdint.h>
 #include <cuda_runtime.h>
 
+#include <utility>
+
 #include "common.cuh"
 
 namespace sp {
+
+// Launch with programmatic stream serialisation when `pdl` (the kernel then
+// calls pdl_wait() before touching its predecessor's data), else normally.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_ex(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool pdl,
+                      Args &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 // Device layout of one database image: one 28-bit residue per (prime,
 // combo, row, slot), where combo m = t*cols + col enumerates the n*n
