@@ -77,3 +77,45 @@ def test_expansion_outputs_by_kernel():
     b32 = bench.expansion_kernel_outputs(p, sh.nu1, sh.nu2, 32)
     assert b32["k_expand_pair"] == 32 * sum(per_round[5:])
     assert b32["k_expand_round<1>"] == 32 * sum(per_round[:5])
+
+
+class _FakeLib:
+    """The calls bench.stage_split makes, recorded."""
+
+    def __init__(self, fail_at=None):
+        self.timing, self.log, self.runs, self.fail_at = False, [], 0, fail_at
+
+    def set_stage_timing(self, on):
+        self.timing = on
+        self.log.append(("timing", on))
+
+    def run_staged(self, count):
+        self.runs += 1
+        if self.runs == self.fail_at:
+            raise RuntimeError("run failed")
+        self.log.append(("run", count, self.timing))
+
+    def stats_reset(self):
+        self.log.append(("reset",))
+
+    def stats(self):
+        return {"ms_expand": 3.0, "ms_total": 6.0, "answers": 3, "db_mul_by_variant": [3, 0, 0]}
+
+
+def test_stage_split_times_with_stage_timing_and_restores_it():
+    """Two capture runs, then the timed runs, all with the library's stage
+    timing on; the ms fields per run; the timing off again afterwards, also
+    when a run fails."""
+    g = _FakeLib()
+    st = bench.stage_split(g, 4, runs=3)
+    assert st["ms_expand"] == 1.0 and st["ms_total"] == 2.0
+    assert st["answers"] == 3 and st["db_mul_by_variant"] == [3, 0, 0]
+    assert g.log[0] == ("timing", True) and g.log[-1] == ("timing", False)
+    assert g.log.index(("reset",)) == 3          # after the two capture runs
+    assert all(e[2] for e in g.log if e[0] == "run") and g.runs == 5
+    bad = _FakeLib(fail_at=4)
+    try:
+        bench.stage_split(bad, 2, runs=3)
+    except RuntimeError:
+        pass
+    assert bad.timing is False
